@@ -1,0 +1,526 @@
+// C ABI of the GB300 FDTD library (declared in include/fdtd_gb300.h):
+// descriptor validation, launch tiling, per-CTA object/source lists and
+// dispatch to the per-precision launch sequences.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "fdtd_kernels.cuh"
+#include "fdtd_plan.hpp"
+
+struct fdtd_plan {
+    fdtd::Plan p;
+};
+
+namespace fdtd {
+
+static thread_local int g_last_cuda = 0;
+void set_last_cuda_error(int e) { g_last_cuda = e; }
+
+static int cuda_fail(cudaError_t e) {
+    g_last_cuda = (int)e;
+    return FDTD_ERR_CUDA;
+}
+
+static int next_pow2(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
+
+static bool box_ok(const int32_t lo[3], const int32_t hi[3], int nx, int ny, int nz) {
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a)
+        if (lo[a] < 0 || hi[a] > n[a] || lo[a] >= hi[a]) return false;
+    return true;
+}
+
+// Ranges of CTA coordinates that a box touches, for the per-CTA lists.
+struct Tiling {
+    int V, TZ, TY, XC, gz, gy, gx;
+};
+
+static void cta_range(const Tiling &t, const int32_t lo[3], const int32_t hi[3], int r[6]) {
+    const int zc = t.V * t.TZ;
+    r[0] = lo[2] / zc;
+    r[1] = (hi[2] - 1) / zc;
+    r[2] = lo[1] / t.TY;
+    r[3] = (hi[1] - 1) / t.TY;
+    r[4] = lo[0] / t.XC;
+    r[5] = (hi[0] - 1) / t.XC;
+}
+
+// CSR lists: for every CTA, the indices (into the device item array) of the
+// items whose box intersects the CTA's cells, in item order.
+static void build_csr(const Tiling &t, const std::vector<ItemK> &items, int first, int count,
+                      std::vector<int> &off, std::vector<int> &idx) {
+    const long ncta = (long)t.gz * t.gy * t.gx;
+    off.assign(ncta + 1, 0);
+    idx.clear();
+    std::vector<int> cnt(ncta, 0);
+    for (int q = first; q < first + count; ++q) {
+        int r[6];
+        cta_range(t, items[q].lo, items[q].hi, r);
+        for (int cx = r[4]; cx <= r[5]; ++cx)
+            for (int cy = r[2]; cy <= r[3]; ++cy)
+                for (int cz = r[0]; cz <= r[1]; ++cz) cnt[cz + t.gz * (cy + (long)t.gy * cx)]++;
+    }
+    for (long c = 0; c < ncta; ++c) off[c + 1] = off[c] + cnt[c];
+    idx.assign(off[ncta], 0);
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (int q = first; q < first + count; ++q) {
+        int r[6];
+        cta_range(t, items[q].lo, items[q].hi, r);
+        for (int cx = r[4]; cx <= r[5]; ++cx)
+            for (int cy = r[2]; cy <= r[3]; ++cy)
+                for (int cz = r[0]; cz <= r[1]; ++cz) idx[fill[cz + t.gz * (cy + (long)t.gy * cx)]++] = q;
+    }
+}
+
+static ItemK to_item(const fdtd_item_desc &d) {
+    ItemK it{};
+    it.kind = d.kind;
+    it.comp = d.comp;
+    it.column = d.column;
+    it.source = d.source;
+    for (int a = 0; a < 3; ++a) {
+        it.lo[a] = d.lo[a];
+        it.hi[a] = d.hi[a];
+    }
+    it.bny = d.hi[1] - d.lo[1];
+    it.bnz = d.hi[2] - d.lo[2];
+    it.weight = d.weight;
+    for (int q = 0; q < 3; ++q) it.coef[q] = d.coef[q];
+    return it;
+}
+
+static bool touches_periodic_plane(const ItemK &it, const std::vector<int> &periodic_axes, const int n[3]) {
+    for (int a : periodic_axes) {
+        if (n[a] <= 1) continue;
+        if (it.lo[a] == 0 || it.hi[a] == n[a]) return true;
+    }
+    return false;
+}
+
+static int create(const fdtd_grid_desc *d, Plan &p) {
+    if (d->abi_version != FDTD_ABI_VERSION) return FDTD_ERR_ARGUMENT;
+    if (d->precision < FDTD_FLOAT32 || d->precision > FDTD_FLOAT64) return FDTD_ERR_ARGUMENT;
+    if (d->nx < 1 || d->ny < 1 || d->nz < 1) return FDTD_ERR_ARGUMENT;
+    if (!d->E || !d->H || !d->inv_eps || !d->inv_mu) return FDTD_ERR_ARGUMENT;
+    const bool comp = d->precision == FDTD_FLOAT32C;
+    if (comp != (d->E_lo != nullptr) || comp != (d->H_lo != nullptr)) return FDTD_ERR_ARGUMENT;
+    if (d->n_boundaries < 0 || d->n_boundaries > FDTD_MAX_BOUNDARIES) return FDTD_ERR_ARGUMENT;
+    if (d->n_objects < 0 || d->n_sources_E < 0 || d->n_sources_H < 0 || d->n_columns < 0 ||
+        d->n_probe_cells < 0 || d->n_dft < 0 || d->n_phase_columns < 0 || d->x_chunk < 0)
+        return FDTD_ERR_ARGUMENT;
+    if ((d->n_objects && !d->objects) || (d->n_sources_E && !d->sources_E) || (d->n_sources_H && !d->sources_H) ||
+        (d->n_probe_cells && !d->probe_cells) || (d->n_dft && !d->dft))
+        return FDTD_ERR_ARGUMENT;
+    const int n[3] = {d->nx, d->ny, d->nz};
+    const size_t esize = d->precision == FDTD_FLOAT64 ? 8 : 4;
+
+    GridK &g = p.k;
+    memset(&g, 0, sizeof(g));
+    p.precision = d->precision;
+    g.nx = d->nx;
+    g.ny = d->ny;
+    g.nz = d->nz;
+    g.courant = d->courant;
+    g.E = d->E;
+    g.H = d->H;
+    g.Elo = d->E_lo;
+    g.Hlo = d->H_lo;
+    g.ie = d->inv_eps;
+    g.imu = d->inv_mu;
+
+    // boundaries: PML slabs in order, periodic axes, the first periodic position
+    int first_periodic = d->n_boundaries;
+    std::vector<int> slab_pos, periodic_axes;
+    for (int b = 0; b < d->n_boundaries; ++b) {
+        const fdtd_boundary_desc &bd = d->boundaries[b];
+        if (bd.axis < 0 || bd.axis > 2) return FDTD_ERR_ARGUMENT;
+        if (bd.kind == FDTD_BOUNDARY_PML) {
+            if (g.nslab >= kMaxSlabs) return FDTD_ERR_UNSUPPORTED;
+            if (bd.thickness < 1 || bd.thickness > n[bd.axis]) return FDTD_ERR_ARGUMENT;
+            if (!bd.psi_E || !bd.psi_H || !bd.b_E || !bd.c_E || !bd.b_H || !bd.c_H) return FDTD_ERR_ARGUMENT;
+            SlabK &S = g.slab[g.nslab];
+            S.axis = bd.axis;
+            S.high = bd.high ? 1 : 0;
+            S.th = bd.thickness;
+            S.start = bd.high ? n[bd.axis] - bd.thickness : 0;
+            S.psiE = bd.psi_E;
+            S.psiH = bd.psi_H;
+            S.bE = bd.b_E;
+            S.cE = bd.c_E;
+            S.bH = bd.b_H;
+            S.cH = bd.c_H;
+            slab_pos.push_back(b);
+            g.nslab++;
+        } else if (bd.kind == FDTD_BOUNDARY_PERIODIC) {
+            if (first_periodic == d->n_boundaries) first_periodic = b;
+            periodic_axes.push_back(bd.axis);
+        } else {
+            return FDTD_ERR_ARGUMENT;
+        }
+    }
+    g.nslab_fused = 0;
+    for (int s = 0; s < g.nslab; ++s)
+        if (slab_pos[s] < first_periodic) g.nslab_fused = s + 1;
+    bool slab_after_periodic = g.nslab_fused < g.nslab;
+    for (int b = first_periodic, s = g.nslab_fused; b < d->n_boundaries; ++b) {
+        const fdtd_boundary_desc &bd = d->boundaries[b];
+        EpiOp op{};
+        if (bd.kind == FDTD_BOUNDARY_PERIODIC) {
+            if (n[bd.axis] <= 1) continue;  // copying a plane onto itself
+            op.kind = EPI_COPY;
+            op.axis = bd.axis;
+        } else {
+            op.kind = EPI_SLAB;
+            op.slab = s++;
+        }
+        p.epi_E.push_back(op);
+        p.epi_H.push_back(op);
+    }
+
+    // tiling
+    const int vmax = d->precision == FDTD_FLOAT64 ? PF64::V : PF32::V;
+    bool vec = (d->nz % vmax) == 0 && aligned16(d->E) && aligned16(d->H) && aligned16(d->inv_eps) &&
+               aligned16(d->inv_mu) && (!comp || (aligned16(d->E_lo) && aligned16(d->H_lo)));
+    Tiling t{};
+    t.V = vec ? vmax : 1;
+    const int zthreads = (d->nz + t.V - 1) / t.V;
+    t.TZ = std::min(32, next_pow2(zthreads));
+    t.TY = kThreads / t.TZ;
+    t.gz = (zthreads + t.TZ - 1) / t.TZ;
+    t.gy = (d->ny + t.TY - 1) / t.TY;
+    if (t.gy > 65535) return FDTD_ERR_UNSUPPORTED;
+    if (d->x_chunk > 0) {
+        t.XC = d->x_chunk;
+    } else {
+        // enough CTAs for about four waves of 152 SMs x 2 resident CTAs
+        const long cols = (long)t.gz * t.gy;
+        long chunks = (4L * 152 * 2 + cols - 1) / cols;
+        chunks = std::max(1L, std::min(chunks, (long)d->nx));
+        t.XC = (int)((d->nx + chunks - 1) / chunks);
+    }
+    t.gx = (d->nx + t.XC - 1) / t.XC;
+    if (t.gx > 65535) return FDTD_ERR_UNSUPPORTED;
+    p.V = t.V;
+    g.TZ = t.TZ;
+    g.TY = t.TY;
+    g.XC = t.XC;
+    p.grid = dim3(t.gz, t.gy, t.gx);
+    p.block = dim3(t.TZ, t.TY, 1);
+
+    // items: objects, E sources, H sources
+    std::vector<ItemK> items;
+    for (int q = 0; q < d->n_objects; ++q) {
+        const fdtd_item_desc &o = d->objects[q];
+        if (o.kind < FDTD_ITEM_OBJECT || o.kind > FDTD_ITEM_ANISOTROPIC) return FDTD_ERR_ARGUMENT;
+        if (!box_ok(o.lo, o.hi, d->nx, d->ny, d->nz) || !o.coef[0]) return FDTD_ERR_ARGUMENT;
+        if (o.kind == FDTD_ITEM_ABSORBING && (!o.coef[1] || (d->precision == FDTD_FLOAT64 && !o.coef[2])))
+            return FDTD_ERR_ARGUMENT;
+        items.push_back(to_item(o));
+    }
+    const int srcE0 = (int)items.size();
+    for (int side = 0; side < 2; ++side) {
+        const int cnt = side == 0 ? d->n_sources_E : d->n_sources_H;
+        const fdtd_item_desc *src = side == 0 ? d->sources_E : d->sources_H;
+        const int begin = (int)items.size();
+        for (int q = 0; q < cnt; ++q) {
+            const fdtd_item_desc &s = src[q];
+            if (s.kind != FDTD_ITEM_SOFT && s.kind != FDTD_ITEM_HARD) return FDTD_ERR_ARGUMENT;
+            if (!box_ok(s.lo, s.hi, d->nx, d->ny, d->nz) || s.comp < 0 || s.comp > 2) return FDTD_ERR_ARGUMENT;
+            if (s.column < 0 || s.column >= d->n_columns) return FDTD_ERR_ARGUMENT;
+            if (s.kind == FDTD_ITEM_SOFT && (s.hi[0] - s.lo[0] != 1 || s.hi[1] - s.lo[1] != 1 || s.hi[2] - s.lo[2] != 1))
+                return FDTD_ERR_ARGUMENT;
+            if (q > 0 && s.source < src[q - 1].source) return FDTD_ERR_ARGUMENT;  // grid.sources order
+            items.push_back(to_item(s));
+        }
+        // within one soft source, order the points by cell (stable: repeated
+        // points keep their order) so that a run of equal cells is contiguous
+        int q = begin;
+        while (q < (int)items.size()) {
+            int e = q + 1;
+            while (e < (int)items.size() && items[e].source == items[q].source) ++e;
+            if (items[q].kind == FDTD_ITEM_SOFT) {
+                std::stable_sort(items.begin() + q, items.begin() + e, [&](const ItemK &x, const ItemK &y) {
+                    const long cx = ((long)x.lo[0] * d->ny + x.lo[1]) * d->nz + x.lo[2];
+                    const long cy = ((long)y.lo[0] * d->ny + y.lo[1]) * d->nz + y.lo[2];
+                    return cx < cy;
+                });
+            }
+            q = e;
+        }
+    }
+    const int srcH0 = srcE0 + d->n_sources_E;
+    const int nitems = (int)items.size();
+
+    // sources inside the fused pass unless a periodic copy must come first
+    const std::vector<ItemK> &cit = items;
+    auto can_fuse = [&](int first, int count) {
+        if (p.epi_E.empty()) return true;
+        if (slab_after_periodic) return false;
+        for (int q = first; q < first + count; ++q)
+            if (touches_periodic_plane(cit[q], periodic_axes, n)) return false;
+        return true;
+    };
+    g.fuse_src_E = can_fuse(srcE0, d->n_sources_E) ? 1 : 0;
+    g.fuse_src_H = can_fuse(srcH0, d->n_sources_H) ? 1 : 0;
+
+    // epilogue source launches and soft runs
+    std::vector<int2> runs;
+    for (int side = 0; side < 2; ++side) {
+        const bool fused = side == 0 ? g.fuse_src_E : g.fuse_src_H;
+        if (fused) continue;
+        const int first = side == 0 ? srcE0 : srcH0;
+        const int last = first + (side == 0 ? d->n_sources_E : d->n_sources_H);
+        std::vector<EpiOp> &ops = side == 0 ? p.epi_E : p.epi_H;
+        int q = first;
+        while (q < last) {
+            int e = q + 1;
+            while (e < last && items[e].source == items[q].source) ++e;
+            if (items[q].kind == FDTD_ITEM_HARD) {
+                for (int h = q; h < e; ++h) {
+                    EpiOp op{};
+                    op.kind = EPI_HARD;
+                    op.item = h;
+                    ops.push_back(op);
+                }
+            } else {
+                EpiOp op{};
+                op.kind = EPI_SOFT;
+                op.run_begin = (int)runs.size();
+                int r = q;
+                while (r < e) {
+                    int re = r + 1;
+                    while (re < e && items[re].lo[0] == items[r].lo[0] && items[re].lo[1] == items[r].lo[1] &&
+                           items[re].lo[2] == items[r].lo[2] && items[re].comp == items[r].comp)
+                        ++re;
+                    runs.push_back(make_int2(r, re - r));
+                    r = re;
+                }
+                op.run_count = (int)runs.size() - op.run_begin;
+                ops.push_back(op);
+            }
+            q = e;
+        }
+    }
+
+    std::vector<int> obj_off, obj_idx, se_off, se_idx, sh_off, sh_idx;
+    build_csr(t, items, 0, srcE0, obj_off, obj_idx);
+    build_csr(t, items, srcE0, d->n_sources_E, se_off, se_idx);
+    build_csr(t, items, srcH0, d->n_sources_H, sh_off, sh_idx);
+
+    // probes and DFT boxes
+    p.n_probe = d->n_probe_cells;
+    p.probe_cells = d->probe_cells;
+    for (int q = 0; q < d->n_dft; ++q) {
+        const fdtd_dft_desc &dd = d->dft[q];
+        if (!box_ok(dd.lo, dd.hi, d->nx, d->ny, d->nz) || dd.n_freq < 1 || !dd.acc || dd.phase_offset < 0 ||
+            dd.phase_offset + dd.n_freq > d->n_phase_columns)
+            return FDTD_ERR_ARGUMENT;
+        p.dft.push_back(dd);
+    }
+    p.n_columns = d->n_columns;
+    p.n_phase_columns = d->n_phase_columns;
+    (void)esize;
+
+    // one device allocation for the plan's tables
+    auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t b_items = align(sizeof(ItemK) * std::max(1, nitems));
+    const size_t b_lists = align(sizeof(int) * (obj_off.size() + obj_idx.size() + se_off.size() + se_idx.size() +
+                                                sh_off.size() + sh_idx.size() + 6));
+    const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
+    std::vector<char> host(b_items + b_lists + b_runs, 0);
+    if (nitems) memcpy(host.data(), items.data(), sizeof(ItemK) * nitems);
+    int *lists = (int *)(host.data() + b_items);
+    size_t pos = 0;
+    size_t at_obj_off, at_obj_idx, at_se_off, at_se_idx, at_sh_off, at_sh_idx;
+    auto put = [&](const std::vector<int> &v, size_t &at) {
+        at = pos;
+        if (!v.empty()) memcpy(lists + pos, v.data(), sizeof(int) * v.size());
+        pos += v.size() + 1;
+    };
+    put(obj_off, at_obj_off);
+    put(obj_idx, at_obj_idx);
+    put(se_off, at_se_off);
+    put(se_idx, at_se_idx);
+    put(sh_off, at_sh_off);
+    put(sh_idx, at_sh_idx);
+    if (!runs.empty()) memcpy(host.data() + b_items + b_lists, runs.data(), sizeof(int2) * runs.size());
+    cudaError_t ce = cudaMalloc(&p.dev_mem, host.size());
+    if (ce != cudaSuccess) return cuda_fail(ce);
+    ce = cudaMemcpy(p.dev_mem, host.data(), host.size(), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        cudaFree(p.dev_mem);
+        p.dev_mem = nullptr;
+        return cuda_fail(ce);
+    }
+    char *base = (char *)p.dev_mem;
+    const int *dl = (const int *)(base + b_items);
+    g.items = (const ItemK *)base;
+    g.obj_off = dl + at_obj_off;
+    g.obj_idx = dl + at_obj_idx;
+    g.srcE_off = dl + at_se_off;
+    g.srcE_idx = dl + at_se_idx;
+    g.srcH_off = dl + at_sh_off;
+    g.srcH_idx = dl + at_sh_idx;
+    p.runs = (const int2 *)(base + b_items + b_lists);
+
+    p.stats_ctas = 152 * 4;
+    p.launches_per_step = 2 + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
+                          (int)p.dft.size();
+    return FDTD_OK;
+}
+
+}  // namespace fdtd
+
+using namespace fdtd;
+
+extern "C" {
+
+int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out) {
+    if (!desc || !out) return FDTD_ERR_ARGUMENT;
+    *out = nullptr;
+    fdtd_plan *h = new fdtd_plan();
+    h->p.dev_mem = nullptr;
+    const int rc = create(desc, h->p);
+    if (rc != FDTD_OK) {
+        if (h->p.dev_mem) cudaFree(h->p.dev_mem);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return FDTD_OK;
+}
+
+int fdtd_plan_destroy(fdtd_plan *plan) {
+    if (!plan) return FDTD_ERR_ARGUMENT;
+    int rc = FDTD_OK;
+    if (plan->p.dev_mem) {
+        cudaError_t e = cudaFree(plan->p.dev_mem);
+        if (e != cudaSuccess) rc = cuda_fail(e);
+    }
+    delete plan;
+    return rc;
+}
+
+int fdtd_run(fdtd_plan *plan, const fdtd_run_args *args, fdtd_stream_t stream) {
+    if (!plan || !args) return FDTD_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (plan->p.precision) {
+        case FDTD_FLOAT32:
+            return run_f32(plan->p, args, st);
+        case FDTD_FLOAT32C:
+            return run_f32c(plan->p, args, st);
+        case FDTD_FLOAT64:
+            return run_f64(plan->p, args, st);
+    }
+    return FDTD_ERR_ARGUMENT;
+}
+
+static int curl_common(int32_t precision, const void *in, void *out, int32_t nx, int32_t ny, int32_t nz,
+                       fdtd_stream_t stream, bool is_E) {
+    if (!in || !out || nx < 1 || ny < 1 || nz < 1) return FDTD_ERR_ARGUMENT;
+    if (precision < FDTD_FLOAT32 || precision > FDTD_FLOAT64) return FDTD_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int blocks = grid_stride_blocks((long)nx * ny * nz);
+    if (precision == FDTD_FLOAT64) {
+        if (is_E) k_curl_E<double><<<blocks, kThreads, 0, st>>>((const double *)in, (double *)out, nx, ny, nz);
+        else k_curl_H<double><<<blocks, kThreads, 0, st>>>((const double *)in, (double *)out, nx, ny, nz);
+    } else {
+        if (is_E) k_curl_E<float><<<blocks, kThreads, 0, st>>>((const float *)in, (float *)out, nx, ny, nz);
+        else k_curl_H<float><<<blocks, kThreads, 0, st>>>((const float *)in, (float *)out, nx, ny, nz);
+    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
+}
+
+int fdtd_curl_E(int32_t precision, const void *E, void *out, int32_t nx, int32_t ny, int32_t nz,
+                fdtd_stream_t stream) {
+    return curl_common(precision, E, out, nx, ny, nz, stream, true);
+}
+
+int fdtd_curl_H(int32_t precision, const void *H, void *out, int32_t nx, int32_t ny, int32_t nz,
+                fdtd_stream_t stream) {
+    return curl_common(precision, H, out, nx, ny, nz, stream, false);
+}
+
+size_t fdtd_stats_scratch_bytes(const fdtd_plan *plan) {
+    if (!plan) return 0;
+    return sizeof(double) * 5 * (size_t)plan->p.stats_ctas;
+}
+
+int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_stream_t stream) {
+    if (!plan || !stats || !scratch) return FDTD_ERR_ARGUMENT;
+    const Plan &p = plan->p;
+    const GridK &g = p.k;
+    const long nvals = 3L * g.nx * g.ny * g.nz;
+    cudaStream_t st = (cudaStream_t)stream;
+    double *part = (double *)scratch;
+    if (p.precision == FDTD_FLOAT64)
+        k_stats_partial<double, false><<<p.stats_ctas, kThreads, 0, st>>>(
+            (const double *)g.E, nullptr, (const double *)g.H, nullptr, nvals, part);
+    else if (p.precision == FDTD_FLOAT32C)
+        k_stats_partial<float, true><<<p.stats_ctas, kThreads, 0, st>>>(
+            (const float *)g.E, (const float *)g.Elo, (const float *)g.H, (const float *)g.Hlo, nvals, part);
+    else
+        k_stats_partial<float, false><<<p.stats_ctas, kThreads, 0, st>>>((const float *)g.E, nullptr,
+                                                                         (const float *)g.H, nullptr, nvals, part);
+    k_stats_final<<<1, 32, 0, st>>>(part, p.stats_ctas, stats);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
+}
+
+int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out6) {
+    if (!plan || !out6) return FDTD_ERR_ARGUMENT;
+    const Plan &p = plan->p;
+    out6[0] = p.V;
+    out6[1] = p.k.TZ;
+    out6[2] = p.k.TY;
+    out6[3] = p.k.XC;
+    out6[4] = (int64_t)p.grid.x * p.grid.y * p.grid.z;
+    out6[5] = p.launches_per_step;
+    return FDTD_OK;
+}
+
+const char *fdtd_status_string(int32_t status) {
+    switch (status) {
+        case FDTD_OK:
+            return "ok";
+        case FDTD_ERR_ARGUMENT:
+            return "invalid argument";
+        case FDTD_ERR_UNSUPPORTED:
+            return "unsupported configuration";
+        case FDTD_ERR_CUDA:
+            return "CUDA error";
+        case FDTD_ERR_NONFINITE:
+            return "non-finite field value";
+        case FDTD_ERR_RANGE:
+            return "out of range";
+    }
+    return "unknown status";
+}
+
+int32_t fdtd_last_cuda_error(void) { return g_last_cuda; }
+
+size_t fdtd_abi_sizeof(int32_t which) {
+    switch (which) {
+        case 0:
+            return sizeof(fdtd_grid_desc);
+        case 1:
+            return sizeof(fdtd_boundary_desc);
+        case 2:
+            return sizeof(fdtd_item_desc);
+        case 3:
+            return sizeof(fdtd_dft_desc);
+        case 4:
+            return sizeof(fdtd_run_args);
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,208 @@
+// Shared device-side definitions of the GB300 FDTD time-step library.
+//
+// Layout: every field is component-last, element (i, j, k, c) at
+// ((i*ny + j)*nz + k)*3 + c.  A thread owns V consecutive cells along z
+// (3*V contiguous values = three 16-byte vectors when V = 4 floats or
+// V = 2 doubles) and marches along x over a chunk of planes, keeping the
+// previous plane of the neighbour field in registers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fdtd_gb300.h"
+
+namespace fdtd {
+
+constexpr int kMaxSlabs = 6;
+constexpr int kThreads = 256;
+
+// One PML slab as the kernels see it.  `start` is the global index of the
+// slab-local plane 0 along `axis`.
+struct SlabK {
+    int axis, high, th, start;
+    void *psiE, *psiH;
+    const void *bE, *cE, *bH, *cH;
+};
+
+// An object or source box on the device.  bny/bnz are the box extents used
+// for box-local coefficient indexing.
+struct ItemK {
+    int kind, comp, column, source;
+    int lo[3], hi[3];
+    int bny, bnz;
+    double weight;
+    const void *coef[3];
+};
+
+// Everything a half-step kernel needs, passed by value.
+struct GridK {
+    int nx, ny, nz;
+    double courant;
+    void *E, *H, *Elo, *Hlo;
+    const void *ie, *imu;
+    int nslab;        // PML slabs in boundary order
+    int nslab_fused;  // slabs [0, nslab_fused) are corrected inside the fused pass
+    SlabK slab[kMaxSlabs];
+    const ItemK *items;
+    const int *obj_off, *obj_idx;    // per-CTA object lists (E half only)
+    const int *srcE_off, *srcE_idx;  // per-CTA source lists
+    const int *srcH_off, *srcH_idx;
+    int fuse_src_E, fuse_src_H;      // sources applied inside the fused pass
+    int TZ, TY, XC;                  // threads along z, rows along y, planes along x per CTA
+};
+
+// ---------------------------------------------------------------------------
+// Precision policies.  The float64 policy reproduces the reference's numpy
+// operation order with explicitly rounded operations (no fused multiply-add),
+// so a float64 plan matches the reference bit for bit wherever the reference
+// order is a plain sequence of elementwise operations.
+// ---------------------------------------------------------------------------
+struct PF64 {
+    using T = double;
+    static constexpr bool COMP = false;
+    static constexpr int V = 2;
+    __device__ __forceinline__ static T mul(T a, T b) { return __dmul_rn(a, b); }
+    __device__ __forceinline__ static void add_prod(T &x, T &, T a, T b) {
+        x = __dadd_rn(x, __dmul_rn(a, b));
+    }
+    __device__ __forceinline__ static void sub_prod(T &x, T &, T a, T b) {
+        x = __dsub_rn(x, __dmul_rn(a, b));
+    }
+    __device__ __forceinline__ static void scale(T &x, T &, T r) { x = __dmul_rn(x, r); }
+    __device__ __forceinline__ static void set(T &x, T &, T v) { x = v; }
+    // x += (a*b)/d, the AbsorbingObject order
+    __device__ __forceinline__ static void add_quot(T &x, T &, T a, T b, T d) {
+        x = __dadd_rn(x, __ddiv_rn(__dmul_rn(a, b), d));
+    }
+    __device__ __forceinline__ static T psi(T p, T b, T d, T c) {
+        return __dadd_rn(__dmul_rn(p, b), __dmul_rn(d, c));
+    }
+    __device__ __forceinline__ static T dot3(T a0, T a1, T a2, T b0, T b1, T b2) {
+        return __dadd_rn(__dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
+    }
+    __device__ __forceinline__ static void finish(T &, T &) {}
+};
+
+struct PF32 {
+    using T = float;
+    static constexpr bool COMP = false;
+    static constexpr int V = 4;
+    __device__ __forceinline__ static T mul(T a, T b) { return a * b; }
+    __device__ __forceinline__ static void add_prod(T &x, T &, T a, T b) { x = fmaf(a, b, x); }
+    __device__ __forceinline__ static void sub_prod(T &x, T &, T a, T b) { x = fmaf(-a, b, x); }
+    __device__ __forceinline__ static void scale(T &x, T &, T r) { x = x * r; }
+    __device__ __forceinline__ static void set(T &x, T &, T v) { x = v; }
+    __device__ __forceinline__ static void add_quot(T &x, T &, T a, T b, T) { x = fmaf(a, b, x); }
+    __device__ __forceinline__ static T psi(T p, T b, T d, T c) { return fmaf(d, c, p * b); }
+    __device__ __forceinline__ static T dot3(T a0, T a1, T a2, T b0, T b1, T b2) {
+        return fmaf(a2, b2, fmaf(a1, b1, a0 * b0));
+    }
+    __device__ __forceinline__ static void finish(T &, T &) {}
+};
+
+// Two-float accumulation: a field value is hi + lo.  Every update that adds
+// to or scales the value keeps the rounding error of that operation in lo
+// (TwoSum for additions, an FMA residual for products), so round-off does
+// not accumulate over long runs.  Stencil differences read hi only.
+struct PF32C {
+    using T = float;
+    static constexpr bool COMP = true;
+    static constexpr int V = 4;
+    __device__ __forceinline__ static void two_sum(T a, T b, T &s, T &e) {
+        s = a + b;
+        T bp = s - a;
+        T ap = s - bp;
+        e = (a - ap) + (b - bp);
+    }
+    __device__ __forceinline__ static T mul(T a, T b) { return a * b; }
+    __device__ __forceinline__ static void add_prod(T &x, T &lo, T a, T b) {
+        T p = a * b;
+        T pe = fmaf(a, b, -p);
+        T s, e;
+        two_sum(x, p, s, e);
+        x = s;
+        lo = lo + (e + pe);
+    }
+    __device__ __forceinline__ static void sub_prod(T &x, T &lo, T a, T b) { add_prod(x, lo, -a, b); }
+    __device__ __forceinline__ static void scale(T &x, T &lo, T r) {
+        T p = x * r;
+        T pe = fmaf(x, r, -p);
+        lo = fmaf(lo, r, pe);
+        x = p;
+    }
+    __device__ __forceinline__ static void set(T &x, T &lo, T v) {
+        x = v;
+        lo = 0.0f;
+    }
+    __device__ __forceinline__ static void add_quot(T &x, T &lo, T a, T b, T) { add_prod(x, lo, a, b); }
+    __device__ __forceinline__ static T psi(T p, T b, T d, T c) { return fmaf(d, c, p * b); }
+    __device__ __forceinline__ static T dot3(T a0, T a1, T a2, T b0, T b1, T b2) {
+        return fmaf(a2, b2, fmaf(a1, b1, a0 * b0));
+    }
+    __device__ __forceinline__ static void finish(T &x, T &lo) {
+        T s, e;
+        two_sum(x, lo, s, e);
+        x = s;
+        lo = e;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Loads and stores of N contiguous values; 16-byte vectors when N*sizeof(T)
+// is a multiple of 16 (the caller guarantees 16-byte alignment then).
+// ---------------------------------------------------------------------------
+template <class T, int N>
+__device__ __forceinline__ void ld_vec(T (&dst)[N], const T *p) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+        for (int i = 0; i < (int)(N * sizeof(T) / 16); ++i) {
+            uint4 t = q[i];
+            *reinterpret_cast<uint4 *>(&dst[i * 16 / sizeof(T)]) = t;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) dst[i] = p[i];
+    }
+}
+
+// Read-only (non-coherent path) variant, only for data the kernel never writes.
+template <class T, int N>
+__device__ __forceinline__ void ld_vec_ro(T (&dst)[N], const T *__restrict__ p) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+        for (int i = 0; i < (int)(N * sizeof(T) / 16); ++i) {
+            uint4 t = __ldg(q + i);
+            *reinterpret_cast<uint4 *>(&dst[i * 16 / sizeof(T)]) = t;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) dst[i] = __ldg(p + i);
+    }
+}
+
+template <class T, int N>
+__device__ __forceinline__ void st_vec(T *p, const T (&src)[N]) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        uint4 *q = reinterpret_cast<uint4 *>(p);
+#pragma unroll
+        for (int i = 0; i < (int)(N * sizeof(T) / 16); ++i)
+            q[i] = *reinterpret_cast<const uint4 *>(&src[i * 16 / sizeof(T)]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = src[i];
+    }
+}
+
+__device__ __forceinline__ bool in_box(const ItemK &it, int i, int j, int k) {
+    return i >= it.lo[0] && i < it.hi[0] && j >= it.lo[1] && j < it.hi[1] && k >= it.lo[2] &&
+           k < it.hi[2];
+}
+
+__device__ __forceinline__ size_t box_index(const ItemK &it, int i, int j, int k) {
+    return ((size_t)(i - it.lo[0]) * it.bny + (j - it.lo[1])) * it.bnz + (k - it.lo[2]);
+}
+
+}  // namespace fdtd

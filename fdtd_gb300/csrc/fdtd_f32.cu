@@ -1,0 +1,7 @@
+// float32 and compensated float32 instantiations of the time-step kernels.
+#include "fdtd_launch.cuh"
+
+namespace fdtd {
+int run_f32(Plan &p, const fdtd_run_args *a, cudaStream_t st) { return run_impl<PF32>(p, a, st); }
+int run_f32c(Plan &p, const fdtd_run_args *a, cudaStream_t st) { return run_impl<PF32C>(p, a, st); }
+}  // namespace fdtd

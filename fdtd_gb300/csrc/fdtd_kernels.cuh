@@ -1,0 +1,615 @@
+// Kernels of the GB300 FDTD time step.
+//
+// k_update_E / k_update_H are the fused half steps.  One pass per half step
+// does, per cell and in the reference's order (fdtd/grid.py:275-325):
+//   PML auxiliary update (fdtd/boundaries.py:433-487, slab-local index rules)
+//   Yee curl (fdtd/grid.py:29-76, out-of-grid differences dropped)
+//   bulk update E += c*eps^-1*curlH / H -= c*mu^-1*curlE
+//   objects in registration order (fdtd/objects.py:118-277)
+//   PML corrections in boundary order (fdtd/boundaries.py:409-431)
+//   sources in registration order (fdtd/sources.py:93-109,278-297,476-486)
+// A CTA covers TZ*V cells along z, TY rows along y and XC planes along x; a
+// thread streams along x holding the neighbour plane in registers.
+#pragma once
+
+#include "fdtd_common.cuh"
+
+namespace fdtd {
+
+#define FULL_MASK 0xffffffffu
+
+template <class P, int V>
+__global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const double *__restrict__ wave) {
+    using T = typename P::T;
+    constexpr int N = 3 * V;
+    const int tz = threadIdx.x, ty = threadIdx.y;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int k0 = (blockIdx.x * g.TZ + tz) * V;
+    const int j = blockIdx.y * g.TY + ty;
+    const int xa = blockIdx.z * g.XC;
+    const int xb = min(nx, xa + g.XC);
+    const bool act = (j < ny) && (k0 < nz);
+    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const T c = (T)g.courant;
+    const T *__restrict__ H = (const T *)g.H;
+    T *E = (T *)g.E;
+    T *Elo = (T *)g.Elo;
+    const T *__restrict__ IE = (const T *)g.ie;
+    const int ob0 = g.obj_off[cta], ob1 = g.obj_off[cta + 1];
+    int sb0 = 0, sb1 = 0;
+    if (g.fuse_src_E) {
+        sb0 = g.srcE_off[cta];
+        sb1 = g.srcE_off[cta + 1];
+    }
+
+    alignas(16) T hp[N];  // H at plane i-1
+#pragma unroll
+    for (int q = 0; q < N; ++q) hp[q] = T(0);
+    if (act && xa > 0) ld_vec_ro(hp, H + 3 * (((size_t)(xa - 1) * ny + j) * nz + k0));
+
+    for (int i = xa; i < xb; ++i) {
+        const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
+        alignas(16) T hc[N], hj[N], e[N], el[N], m[N];
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            hc[q] = T(0);
+            hj[q] = T(0);
+            e[q] = T(0);
+            el[q] = T(0);
+            m[q] = T(0);
+        }
+        if (act) {
+            ld_vec_ro(hc, H + 3 * cell0);
+            if (j > 0) ld_vec_ro(hj, H + 3 * (cell0 - nz));
+            ld_vec(e, E + 3 * cell0);
+            if constexpr (P::COMP) ld_vec(el, Elo + 3 * cell0);
+            ld_vec_ro(m, IE + 3 * cell0);
+        }
+        // (Hx, Hy) at k0-1: from the lane to the left, or from memory at a row start
+        T kx = __shfl_up_sync(FULL_MASK, hc[N - 3], 1);
+        T ky = __shfl_up_sync(FULL_MASK, hc[N - 2], 1);
+        if (tz == 0 && act && k0 > 0) {
+            kx = H[3 * (cell0 - 1)];
+            ky = H[3 * (cell0 - 1) + 1];
+        }
+        if (act) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int k = k0 + v;
+                const T hx = hc[3 * v], hy = hc[3 * v + 1], hz = hc[3 * v + 2];
+                const T pkx = (v > 0) ? hc[3 * (v - 1)] : kx;
+                const T pky = (v > 0) ? hc[3 * (v - 1) + 1] : ky;
+                // backward differences; zero on the first plane of their axis
+                const T dxHy = (i > 0) ? hy - hp[3 * v + 1] : T(0);
+                const T dxHz = (i > 0) ? hz - hp[3 * v + 2] : T(0);
+                const T dyHx = (j > 0) ? hx - hj[3 * v] : T(0);
+                const T dyHz = (j > 0) ? hz - hj[3 * v + 2] : T(0);
+                const T dzHx = (k > 0) ? hx - pkx : T(0);
+                const T dzHy = (k > 0) ? hy - pky : T(0);
+                const T cu0 = dyHz - dzHy;
+                const T cu1 = dzHx - dxHz;
+                const T cu2 = dxHy - dyHx;
+                T ex = e[3 * v], ey = e[3 * v + 1], ez = e[3 * v + 2];
+                T lx = el[3 * v], ly = el[3 * v + 1], lz = el[3 * v + 2];
+                const T m0 = m[3 * v], m1 = m[3 * v + 1], m2 = m[3 * v + 2];
+                P::add_prod(ex, lx, P::mul(c, m0), cu0);
+                P::add_prod(ey, ly, P::mul(c, m1), cu1);
+                P::add_prod(ez, lz, P::mul(c, m2), cu2);
+
+                for (int it = ob0; it < ob1; ++it) {
+                    const ItemK &o = g.items[g.obj_idx[it]];
+                    if (!in_box(o, i, j, k)) continue;
+                    const size_t li = box_index(o, i, j, k);
+                    if (o.kind == FDTD_ITEM_OBJECT) {
+                        const T *cf = (const T *)o.coef[0] + 3 * li;
+                        P::add_prod(ex, lx, cf[0], cu0);
+                        P::add_prod(ey, ly, cf[1], cu1);
+                        P::add_prod(ez, lz, cf[2], cu2);
+                    } else if (o.kind == FDTD_ITEM_ABSORBING) {
+                        const T *r = (const T *)o.coef[0] + 3 * li;
+                        const T *ci = (const T *)o.coef[1] + 3 * li;
+                        P::scale(ex, lx, r[0]);
+                        P::scale(ey, ly, r[1]);
+                        P::scale(ez, lz, r[2]);
+                        if constexpr (P::COMP || sizeof(T) == 4) {
+                            P::add_prod(ex, lx, ci[0], cu0);
+                            P::add_prod(ey, ly, ci[1], cu1);
+                            P::add_prod(ez, lz, ci[2], cu2);
+                        } else {
+                            const T *opf = (const T *)o.coef[2] + 3 * li;
+                            P::add_quot(ex, lx, ci[0], cu0, opf[0]);
+                            P::add_quot(ey, ly, ci[1], cu1, opf[1]);
+                            P::add_quot(ez, lz, ci[2], cu2, opf[2]);
+                        }
+                    } else {
+                        const T *M = (const T *)o.coef[0] + 9 * li;
+                        P::add_prod(ex, lx, c, P::dot3(M[0], M[1], M[2], cu0, cu1, cu2));
+                        P::add_prod(ey, ly, c, P::dot3(M[3], M[4], M[5], cu0, cu1, cu2));
+                        P::add_prod(ez, lz, c, P::dot3(M[6], M[7], M[8], cu0, cu1, cu2));
+                    }
+                }
+
+                for (int s = 0; s < g.nslab; ++s) {
+                    const SlabK &S = g.slab[s];
+                    const int a = S.axis;
+                    const int l = (a == 0 ? i : (a == 1 ? j : k)) - S.start;
+                    if ((unsigned)l >= (unsigned)S.th) continue;
+                    const size_t pidx = a == 0   ? ((size_t)l * ny + j) * nz + k
+                                        : a == 1 ? ((size_t)i * S.th + l) * nz + k
+                                                 : ((size_t)i * ny + j) * S.th + l;
+                    T *pp = (T *)S.psiE + 2 * pidx;
+                    T p0 = pp[0], p1 = pp[1];
+                    const T b = ((const T *)S.bE)[l];
+                    if (l >= 1) {
+                        const T cc = ((const T *)S.cE)[l];
+                        const T d0 = a == 0 ? dxHz : (a == 1 ? dyHx : dzHy);
+                        const T d1 = a == 0 ? dxHy : (a == 1 ? dyHz : dzHx);
+                        p0 = P::psi(p0, b, d0, cc);
+                        p1 = P::psi(p1, b, d1, cc);
+                    } else {
+                        p0 = P::mul(p0, b);
+                        p1 = P::mul(p1, b);
+                    }
+                    pp[0] = p0;
+                    pp[1] = p1;
+                    if (s < g.nslab_fused) {
+                        if (a == 0) {
+                            P::add_prod(ey, ly, P::mul(c, m1), -p0);
+                            P::add_prod(ez, lz, P::mul(c, m2), p1);
+                        } else if (a == 1) {
+                            P::add_prod(ez, lz, P::mul(c, m2), -p0);
+                            P::add_prod(ex, lx, P::mul(c, m0), p1);
+                        } else {
+                            P::add_prod(ex, lx, P::mul(c, m0), -p0);
+                            P::add_prod(ey, ly, P::mul(c, m1), p1);
+                        }
+                    }
+                }
+
+                for (int it = sb0; it < sb1; ++it) {
+                    const ItemK &s = g.items[g.srcE_idx[it]];
+                    if (!in_box(s, i, j, k)) continue;
+                    const T w = (T)s.weight, wv = (T)wave[s.column];
+                    if (s.kind == FDTD_ITEM_SOFT) {
+                        if (s.comp == 0) P::add_prod(ex, lx, w, wv);
+                        else if (s.comp == 1) P::add_prod(ey, ly, w, wv);
+                        else P::add_prod(ez, lz, w, wv);
+                    } else {
+                        const T val = P::mul(w, wv);
+                        if (s.comp == 0) P::set(ex, lx, val);
+                        else if (s.comp == 1) P::set(ey, ly, val);
+                        else P::set(ez, lz, val);
+                    }
+                }
+                P::finish(ex, lx);
+                P::finish(ey, ly);
+                P::finish(ez, lz);
+                e[3 * v] = ex;
+                e[3 * v + 1] = ey;
+                e[3 * v + 2] = ez;
+                el[3 * v] = lx;
+                el[3 * v + 1] = ly;
+                el[3 * v + 2] = lz;
+            }
+            st_vec(E + 3 * cell0, e);
+            if constexpr (P::COMP) st_vec(Elo + 3 * cell0, el);
+        }
+#pragma unroll
+        for (int q = 0; q < N; ++q) hp[q] = hc[q];
+    }
+}
+
+template <class P, int V>
+__global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const double *__restrict__ wave) {
+    using T = typename P::T;
+    constexpr int N = 3 * V;
+    const int tz = threadIdx.x, ty = threadIdx.y;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int k0 = (blockIdx.x * g.TZ + tz) * V;
+    const int j = blockIdx.y * g.TY + ty;
+    const int xa = blockIdx.z * g.XC;
+    const int xb = min(nx, xa + g.XC);
+    const bool act = (j < ny) && (k0 < nz);
+    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const T c = (T)g.courant;
+    const T *__restrict__ E = (const T *)g.E;
+    T *H = (T *)g.H;
+    T *Hlo = (T *)g.Hlo;
+    const T *__restrict__ MU = (const T *)g.imu;
+    int sb0 = 0, sb1 = 0;
+    if (g.fuse_src_H) {
+        sb0 = g.srcH_off[cta];
+        sb1 = g.srcH_off[cta + 1];
+    }
+
+    alignas(16) T ec[N];  // E at plane i
+#pragma unroll
+    for (int q = 0; q < N; ++q) ec[q] = T(0);
+    if (act && xa < xb) ld_vec_ro(ec, E + 3 * (((size_t)xa * ny + j) * nz + k0));
+
+    for (int i = xa; i < xb; ++i) {
+        const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
+        alignas(16) T en[N], ej[N], h[N], hl[N], m[N];
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            en[q] = T(0);
+            ej[q] = T(0);
+            h[q] = T(0);
+            hl[q] = T(0);
+            m[q] = T(0);
+        }
+        if (act) {
+            if (i + 1 < nx) ld_vec_ro(en, E + 3 * (cell0 + (size_t)ny * nz));
+            if (j + 1 < ny) ld_vec_ro(ej, E + 3 * (cell0 + nz));
+            ld_vec(h, H + 3 * cell0);
+            if constexpr (P::COMP) ld_vec(hl, Hlo + 3 * cell0);
+            ld_vec_ro(m, MU + 3 * cell0);
+        }
+        // (Ex, Ey) at k0+V: from the lane to the right, or from memory at a row end
+        T kx = __shfl_down_sync(FULL_MASK, ec[0], 1);
+        T ky = __shfl_down_sync(FULL_MASK, ec[1], 1);
+        if (tz == g.TZ - 1 && act && k0 + V < nz) {
+            kx = E[3 * (cell0 + V)];
+            ky = E[3 * (cell0 + V) + 1];
+        }
+        if (act) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int k = k0 + v;
+                const T ex_ = ec[3 * v], ey_ = ec[3 * v + 1], ez_ = ec[3 * v + 2];
+                const T nkx = (v < V - 1) ? ec[3 * (v + 1)] : kx;
+                const T nky = (v < V - 1) ? ec[3 * (v + 1) + 1] : ky;
+                // forward differences; zero on the last plane of their axis
+                const T dxEy = (i < nx - 1) ? en[3 * v + 1] - ey_ : T(0);
+                const T dxEz = (i < nx - 1) ? en[3 * v + 2] - ez_ : T(0);
+                const T dyEx = (j < ny - 1) ? ej[3 * v] - ex_ : T(0);
+                const T dyEz = (j < ny - 1) ? ej[3 * v + 2] - ez_ : T(0);
+                const T dzEx = (k < nz - 1) ? nkx - ex_ : T(0);
+                const T dzEy = (k < nz - 1) ? nky - ey_ : T(0);
+                const T cu0 = dyEz - dzEy;
+                const T cu1 = dzEx - dxEz;
+                const T cu2 = dxEy - dyEx;
+                T hx = h[3 * v], hy = h[3 * v + 1], hz = h[3 * v + 2];
+                T lx = hl[3 * v], ly = hl[3 * v + 1], lz = hl[3 * v + 2];
+                const T m0 = m[3 * v], m1 = m[3 * v + 1], m2 = m[3 * v + 2];
+                P::sub_prod(hx, lx, P::mul(c, m0), cu0);
+                P::sub_prod(hy, ly, P::mul(c, m1), cu1);
+                P::sub_prod(hz, lz, P::mul(c, m2), cu2);
+
+                for (int s = 0; s < g.nslab; ++s) {
+                    const SlabK &S = g.slab[s];
+                    const int a = S.axis;
+                    const int l = (a == 0 ? i : (a == 1 ? j : k)) - S.start;
+                    if ((unsigned)l >= (unsigned)S.th) continue;
+                    const size_t pidx = a == 0   ? ((size_t)l * ny + j) * nz + k
+                                        : a == 1 ? ((size_t)i * S.th + l) * nz + k
+                                                 : ((size_t)i * ny + j) * S.th + l;
+                    T *pp = (T *)S.psiH + 2 * pidx;
+                    T p0 = pp[0], p1 = pp[1];
+                    const T b = ((const T *)S.bH)[l];
+                    if (l <= S.th - 2) {
+                        const T cc = ((const T *)S.cH)[l];
+                        const T d0 = a == 0 ? dxEz : (a == 1 ? dyEx : dzEy);
+                        const T d1 = a == 0 ? dxEy : (a == 1 ? dyEz : dzEx);
+                        p0 = P::psi(p0, b, d0, cc);
+                        p1 = P::psi(p1, b, d1, cc);
+                    } else {
+                        p0 = P::mul(p0, b);
+                        p1 = P::mul(p1, b);
+                    }
+                    pp[0] = p0;
+                    pp[1] = p1;
+                    if (s < g.nslab_fused) {
+                        if (a == 0) {
+                            P::sub_prod(hy, ly, P::mul(c, m1), -p0);
+                            P::sub_prod(hz, lz, P::mul(c, m2), p1);
+                        } else if (a == 1) {
+                            P::sub_prod(hz, lz, P::mul(c, m2), -p0);
+                            P::sub_prod(hx, lx, P::mul(c, m0), p1);
+                        } else {
+                            P::sub_prod(hx, lx, P::mul(c, m0), -p0);
+                            P::sub_prod(hy, ly, P::mul(c, m1), p1);
+                        }
+                    }
+                }
+
+                for (int it = sb0; it < sb1; ++it) {
+                    const ItemK &s = g.items[g.srcH_idx[it]];
+                    if (!in_box(s, i, j, k)) continue;
+                    const T w = (T)s.weight, wv = (T)wave[s.column];
+                    if (s.kind == FDTD_ITEM_SOFT) {
+                        if (s.comp == 0) P::add_prod(hx, lx, w, wv);
+                        else if (s.comp == 1) P::add_prod(hy, ly, w, wv);
+                        else P::add_prod(hz, lz, w, wv);
+                    } else {
+                        const T val = P::mul(w, wv);
+                        if (s.comp == 0) P::set(hx, lx, val);
+                        else if (s.comp == 1) P::set(hy, ly, val);
+                        else P::set(hz, lz, val);
+                    }
+                }
+                P::finish(hx, lx);
+                P::finish(hy, ly);
+                P::finish(hz, lz);
+                h[3 * v] = hx;
+                h[3 * v + 1] = hy;
+                h[3 * v + 2] = hz;
+                hl[3 * v] = lx;
+                hl[3 * v + 1] = ly;
+                hl[3 * v + 2] = lz;
+            }
+            st_vec(H + 3 * cell0, h);
+            if constexpr (P::COMP) st_vec(Hlo + 3 * cell0, hl);
+        }
+#pragma unroll
+        for (int q = 0; q < N; ++q) ec[q] = en[q];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels used when a periodic boundary fixes the order of the stages
+// after the fused pass, plus detectors, DFT, stand-alone curls and stats.
+// ---------------------------------------------------------------------------
+
+// Periodic plane copy (fdtd/boundaries.py:184-219): F[plane dst] = F[plane src].
+template <class T, bool COMP>
+__global__ void k_plane_copy(T *F, T *Flo, int nx, int ny, int nz, int axis, int dst, int src) {
+    const int n1 = axis == 0 ? ny : nx;
+    const int n2 = axis == 2 ? ny : nz;
+    const long total = (long)n1 * n2 * 3;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int comp = (int)(t % 3);
+        const long pc = t / 3;
+        const int a = (int)(pc / n2), b = (int)(pc % n2);
+        size_t cd, cs;
+        if (axis == 0) {
+            cd = ((size_t)dst * ny + a) * nz + b;
+            cs = ((size_t)src * ny + a) * nz + b;
+        } else if (axis == 1) {
+            cd = ((size_t)a * ny + dst) * nz + b;
+            cs = ((size_t)a * ny + src) * nz + b;
+        } else {
+            cd = ((size_t)a * ny + b) * nz + dst;
+            cs = ((size_t)a * ny + b) * nz + src;
+        }
+        F[3 * cd + comp] = F[3 * cs + comp];
+        if constexpr (COMP) Flo[3 * cd + comp] = Flo[3 * cs + comp];
+    }
+}
+
+// PML correction of one slab on its own (boundary after a periodic boundary).
+template <class P, bool IS_E>
+__global__ void k_slab_correct(const GridK g, int s) {
+    using T = typename P::T;
+    const SlabK &S = g.slab[s];
+    const int a = S.axis;
+    const int n0 = a == 0 ? S.th : g.nx, n1 = a == 1 ? S.th : g.ny, n2 = a == 2 ? S.th : g.nz;
+    const long total = (long)n0 * n1 * n2;
+    const T c = (T)g.courant;
+    T *F = (T *)(IS_E ? g.E : g.H);
+    T *Flo = (T *)(IS_E ? g.Elo : g.Hlo);
+    const T *M = (const T *)(IS_E ? g.ie : g.imu);
+    const T *psi = (const T *)(IS_E ? S.psiE : S.psiH);
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i0 = (int)(t / ((long)n1 * n2)), i1 = (int)((t / n2) % n1), i2 = (int)(t % n2);
+        const int gi = a == 0 ? i0 + S.start : i0, gj = a == 1 ? i1 + S.start : i1, gk = a == 2 ? i2 + S.start : i2;
+        const size_t cell = ((size_t)gi * g.ny + gj) * g.nz + gk;
+        const T p0 = psi[2 * t], p1 = psi[2 * t + 1];
+        const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+        T x1 = F[3 * cell + t1], x2 = F[3 * cell + t2];
+        T l1 = T(0), l2 = T(0);
+        if constexpr (P::COMP) {
+            l1 = Flo[3 * cell + t1];
+            l2 = Flo[3 * cell + t2];
+        }
+        const T c1 = P::mul(c, M[3 * cell + t1]), c2 = P::mul(c, M[3 * cell + t2]);
+        if (IS_E) {
+            P::add_prod(x1, l1, c1, -p0);
+            P::add_prod(x2, l2, c2, p1);
+        } else {
+            P::sub_prod(x1, l1, c1, -p0);
+            P::sub_prod(x2, l2, c2, p1);
+        }
+        P::finish(x1, l1);
+        P::finish(x2, l2);
+        F[3 * cell + t1] = x1;
+        F[3 * cell + t2] = x2;
+        if constexpr (P::COMP) {
+            Flo[3 * cell + t1] = l1;
+            Flo[3 * cell + t2] = l2;
+        }
+    }
+}
+
+// Soft source points applied on their own: one thread per run of items that
+// share a cell, applied in order (a LineSource may list a cell twice).
+template <class P>
+__global__ void k_soft_runs(const GridK g, const int2 *runs, int nruns, const double *wave, int field) {
+    using T = typename P::T;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    T *F = (T *)(field == 0 ? g.E : g.H);
+    T *Flo = (T *)(field == 0 ? g.Elo : g.Hlo);
+    const int2 run = runs[r];
+    const ItemK &first = g.items[run.x];
+    const size_t cell = ((size_t)first.lo[0] * g.ny + first.lo[1]) * g.nz + first.lo[2];
+    const size_t at = 3 * cell + first.comp;
+    T x = F[at];
+    T lo = T(0);
+    if constexpr (P::COMP) lo = Flo[at];
+    for (int q = 0; q < run.y; ++q) {
+        const ItemK &s = g.items[run.x + q];
+        P::add_prod(x, lo, (T)s.weight, (T)wave[s.column]);
+    }
+    P::finish(x, lo);
+    F[at] = x;
+    if constexpr (P::COMP) Flo[at] = lo;
+}
+
+// Hard source box applied on its own (PlaneSource.update_E/H).
+template <class P>
+__global__ void k_hard_box(const GridK g, int item, const double *wave, int field) {
+    using T = typename P::T;
+    const ItemK &s = g.items[item];
+    const int b0 = s.hi[0] - s.lo[0], b1 = s.hi[1] - s.lo[1], b2 = s.hi[2] - s.lo[2];
+    const long total = (long)b0 * b1 * b2;
+    T *F = (T *)(field == 0 ? g.E : g.H);
+    T *Flo = (T *)(field == 0 ? g.Elo : g.Hlo);
+    const T val = P::mul((T)s.weight, (T)wave[s.column]);
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = s.lo[0] + (int)(t / ((long)b1 * b2)), j = s.lo[1] + (int)((t / b2) % b1),
+                  k = s.lo[2] + (int)(t % b2);
+        const size_t at = 3 * (((size_t)i * g.ny + j) * g.nz + k) + s.comp;
+        F[at] = val;
+        if constexpr (P::COMP) Flo[at] = T(0);
+    }
+}
+
+// Detector sampling: out[p][c] = F[cells[p]][c].
+template <class T>
+__global__ void k_probe(const T *__restrict__ F, const int64_t *__restrict__ cells, int n, T *out) {
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= 3L * n) return;
+    const long p = t / 3;
+    const int comp = (int)(t % 3);
+    out[t] = F[3 * cells[p] + comp];
+}
+
+// Running DFT of E on a box, accumulated in double.
+template <class T, bool COMP>
+__global__ void k_dft(const T *__restrict__ E, const T *__restrict__ Elo, int ny, int nz, fdtd_dft_desc d,
+                      const double *__restrict__ phase) {
+    const int b0 = d.hi[0] - d.lo[0], b1 = d.hi[1] - d.lo[1], b2 = d.hi[2] - d.lo[2];
+    const long ncell = (long)b0 * b1 * b2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < ncell * 3; t += (long)gridDim.x * blockDim.x) {
+        const long cell = t / 3;
+        const int comp = (int)(t % 3);
+        const int i = d.lo[0] + (int)(cell / ((long)b1 * b2)), j = d.lo[1] + (int)((cell / b2) % b1),
+                  k = d.lo[2] + (int)(cell % b2);
+        const size_t at = 3 * (((size_t)i * ny + j) * nz + k) + comp;
+        double e = (double)E[at];
+        if constexpr (COMP) e = e + (double)Elo[at];
+        for (int f = 0; f < d.n_freq; ++f) {
+            const double cs = phase[2 * (d.phase_offset + f)], sn = phase[2 * (d.phase_offset + f) + 1];
+            double *acc = d.acc + 2 * ((size_t)f * ncell * 3 + t);
+            acc[0] = __dadd_rn(acc[0], __dmul_rn(e, cs));
+            acc[1] = __dadd_rn(acc[1], __dmul_rn(e, sn));
+        }
+    }
+}
+
+// Stand-alone curls, one thread per cell (fdtd/grid.py:29-76).
+template <class T>
+__global__ void k_curl_E(const T *__restrict__ E, T *out, int nx, int ny, int nz) {
+    const long n = (long)nx * ny * nz;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / ((long)ny * nz)), j = (int)((t / nz) % ny), k = (int)(t % nz);
+        const T *e = E + 3 * t;
+        const T dxEy = i < nx - 1 ? e[3L * ny * nz + 1] - e[1] : T(0);
+        const T dxEz = i < nx - 1 ? e[3L * ny * nz + 2] - e[2] : T(0);
+        const T dyEx = j < ny - 1 ? e[3L * nz] - e[0] : T(0);
+        const T dyEz = j < ny - 1 ? e[3L * nz + 2] - e[2] : T(0);
+        const T dzEx = k < nz - 1 ? e[3] - e[0] : T(0);
+        const T dzEy = k < nz - 1 ? e[4] - e[1] : T(0);
+        out[3 * t] = dyEz - dzEy;
+        out[3 * t + 1] = dzEx - dxEz;
+        out[3 * t + 2] = dxEy - dyEx;
+    }
+}
+
+template <class T>
+__global__ void k_curl_H(const T *__restrict__ H, T *out, int nx, int ny, int nz) {
+    const long n = (long)nx * ny * nz;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / ((long)ny * nz)), j = (int)((t / nz) % ny), k = (int)(t % nz);
+        const T *h = H + 3 * t;
+        const T dxHy = i > 0 ? h[1] - h[1 - 3L * ny * nz] : T(0);
+        const T dxHz = i > 0 ? h[2] - h[2 - 3L * ny * nz] : T(0);
+        const T dyHx = j > 0 ? h[0] - h[-3L * nz] : T(0);
+        const T dyHz = j > 0 ? h[2] - h[2 - 3L * nz] : T(0);
+        const T dzHx = k > 0 ? h[0] - h[-3] : T(0);
+        const T dzHy = k > 0 ? h[1] - h[-2] : T(0);
+        out[3 * t] = dyHz - dzHy;
+        out[3 * t + 1] = dzHx - dxHz;
+        out[3 * t + 2] = dxHy - dyHx;
+    }
+}
+
+// Field statistics, first pass: one partial row of 5 doubles per CTA.
+template <class T, bool COMP>
+__global__ void __launch_bounds__(kThreads) k_stats_partial(const T *__restrict__ E, const T *__restrict__ Elo,
+                                                            const T *__restrict__ H, const T *__restrict__ Hlo,
+                                                            long nvals, double *partial) {
+    double se = 0.0, sh = 0.0, me = 0.0, mh = 0.0, bad = 0.0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nvals; t += (long)gridDim.x * blockDim.x) {
+        double e = (double)E[t], h = (double)H[t];
+        if constexpr (COMP) {
+            e += (double)Elo[t];
+            h += (double)Hlo[t];
+        }
+        if (!isfinite(e)) bad += 1.0;
+        else {
+            se += e * e;
+            me = fmax(me, fabs(e));
+        }
+        if (!isfinite(h)) bad += 1.0;
+        else {
+            sh += h * h;
+            mh = fmax(mh, fabs(h));
+        }
+    }
+    __shared__ double red[5][kThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        se += __shfl_down_sync(FULL_MASK, se, off);
+        sh += __shfl_down_sync(FULL_MASK, sh, off);
+        me = fmax(me, __shfl_down_sync(FULL_MASK, me, off));
+        mh = fmax(mh, __shfl_down_sync(FULL_MASK, mh, off));
+        bad += __shfl_down_sync(FULL_MASK, bad, off);
+    }
+    if (lane == 0) {
+        red[0][w] = se;
+        red[1][w] = sh;
+        red[2][w] = me;
+        red[3][w] = mh;
+        red[4][w] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0;
+        for (int q = 0; q < kThreads / 32; ++q) {
+            a0 += red[0][q];
+            a1 += red[1][q];
+            a2 = fmax(a2, red[2][q]);
+            a3 = fmax(a3, red[3][q]);
+            a4 += red[4][q];
+        }
+        double *row = partial + 5 * blockIdx.x;
+        row[0] = a0;
+        row[1] = a1;
+        row[2] = a2;
+        row[3] = a3;
+        row[4] = a4;
+    }
+}
+
+// Second pass: one thread folds the CTA rows in order (deterministic).
+static __global__ void k_stats_final(const double *partial, int nrows, double *out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0;
+    for (int r = 0; r < nrows; ++r) {
+        a0 += partial[5 * r];
+        a1 += partial[5 * r + 1];
+        a2 = fmax(a2, partial[5 * r + 2]);
+        a3 = fmax(a3, partial[5 * r + 3]);
+        a4 += partial[5 * r + 4];
+    }
+    out[0] = a0;
+    out[1] = a1;
+    out[2] = a2;
+    out[3] = a3;
+    out[4] = a4;
+}
+
+}  // namespace fdtd

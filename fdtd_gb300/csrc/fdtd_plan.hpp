@@ -1,0 +1,53 @@
+// Host-side plan of the GB300 FDTD library: launch tiling, the fused-pass
+// parameters and the ordered list of small kernels that follow the fused
+// pass when a periodic boundary fixes the order of the later stages.
+#pragma once
+
+#include <vector>
+
+#include "fdtd_common.cuh"
+
+namespace fdtd {
+
+enum EpiKind { EPI_COPY = 0, EPI_SLAB = 1, EPI_SOFT = 2, EPI_HARD = 3 };
+
+struct EpiOp {
+    int kind;
+    int axis;       // EPI_COPY
+    int slab;       // EPI_SLAB
+    int item;       // EPI_HARD
+    int run_begin;  // EPI_SOFT
+    int run_count;
+};
+
+struct Plan {
+    int precision;
+    GridK k;
+    int V;             // cells per thread along z
+    dim3 grid, block;  // fused-pass launch shape
+    std::vector<EpiOp> epi_E, epi_H;
+    const int2 *runs;  // device, soft-source runs for EPI_SOFT
+    int n_probe;
+    const int64_t *probe_cells;
+    std::vector<fdtd_dft_desc> dft;
+    int n_columns, n_phase_columns;
+    void *dev_mem;     // the plan's own device tables
+    int stats_ctas;
+    int launches_per_step;
+};
+
+// Per-precision entry points (one translation unit per precision).
+int run_f32(Plan &p, const fdtd_run_args *a, cudaStream_t st);
+int run_f32c(Plan &p, const fdtd_run_args *a, cudaStream_t st);
+int run_f64(Plan &p, const fdtd_run_args *a, cudaStream_t st);
+
+void set_last_cuda_error(int e);
+
+inline int grid_stride_blocks(long total) {
+    long b = (total + kThreads - 1) / kThreads;
+    if (b < 1) b = 1;
+    if (b > 152L * 16) b = 152L * 16;
+    return (int)b;
+}
+
+}  // namespace fdtd

@@ -1,0 +1,341 @@
+"""Plan compilation and time stepping through the C ABI.
+
+``Engine`` turns a grid's registered components into an ``fdtd_grid_desc``
+(include/fdtd_gb300.h), creates the native plan, and runs steps:
+
+* waveform table -- for a call covering steps q0..q0+n-1 the host evaluates
+  every source's waveform with the reference's Python expressions and copies
+  the (n, n_sources) float64 table to the device through a pinned buffer;
+* detector traces -- one device buffer (capacity, n_probe_cells, 3) in the
+  grid precision, grown geometrically; detectors view their slice of it;
+* DFT phases -- (n, n_freq_total, 2) float64 (cos, -sin) per step.
+
+The plan is rebuilt when components are registered, when an object's
+coefficients change, or when the tiling option changes; detector records
+taken before a rebuild are kept (copied out of the old buffer).
+"""
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _native
+from .boundaries import PML, PeriodicBoundary
+from .detectors import DFTPlaneDetector
+
+_PRECISION = {"float32": _native.FLOAT32, "float32c": _native.FLOAT32C, "float64": _native.FLOAT64}
+
+
+def _require_gpu(grid):
+    if not torch.cuda.is_available():
+        raise RuntimeError("the gb300 backend needs a CUDA device; this machine has none "
+                           "(there is no CPU time step)")
+    if grid._E.device.type != "cuda":
+        raise RuntimeError("this grid was built without a CUDA device; rebuild it on a GPU machine")
+    return _native.load()
+
+
+class _PinnedStager:
+    """Double-buffered pinned host staging for small per-call tables."""
+
+    def __init__(self):
+        self._bufs = [None, None]
+        self._events = [None, None]
+        self._dev = None
+        self._turn = 0
+
+    def upload(self, array, device):
+        n = array.size
+        k = self._turn
+        self._turn ^= 1
+        if self._events[k] is not None:
+            self._events[k].synchronize()
+        if self._bufs[k] is None or self._bufs[k].numel() < n:
+            self._bufs[k] = torch.empty(max(n, 1024), dtype=torch.float64).pin_memory()
+        host = self._bufs[k][:n]
+        host.numpy()[:] = array.reshape(-1)
+        dev = torch.empty(n, dtype=torch.float64, device=device)
+        dev.copy_(host, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self._events[k] = ev
+        return dev
+
+
+class Engine:
+    def __init__(self, grid, x_chunk=0):
+        self.grid = grid
+        self.x_chunk = x_chunk
+        self.plan = None
+        self._key = None
+        self._keep = []
+        self.trace_E = self.trace_H = None
+        self.capacity = 0
+        self.rec_E = self.rec_H = 0
+        self.n_probe = 0
+        self.det_ranges = {}
+        self.dfts = []
+        self.n_phase = 0
+        self._wave_stage = _PinnedStager()
+        self._phase_stage = _PinnedStager()
+        self.launches_per_step = 0
+        self.refresh()
+
+    # --- plan -------------------------------------------------------------------
+    def _state_key(self):
+        g = self.grid
+        return (tuple(o._coef_key() for o in g.objects), self.x_chunk, g.courant_number,
+                g._E.data_ptr(), g._H.data_ptr())
+
+    def refresh(self):
+        g = self.grid
+        key = self._state_key()
+        if self.plan is not None and not g._dirty and key == self._key:
+            return
+        self._build()
+        self._key = self._state_key()
+        g._dirty = False
+
+    def set_x_chunk(self, x_chunk):
+        self.x_chunk = int(x_chunk)
+        self.refresh()
+
+    def tiling(self):
+        """(cells per thread along z, threads along z, rows per CTA, planes per
+        CTA along x, CTAs, kernel launches per step)."""
+        out = (ctypes.c_int64 * 6)()
+        _native.check(_native.load().fdtd_plan_tiling(self.plan, out), "fdtd_plan_tiling")
+        return tuple(out)
+
+    def _freeze_traces(self):
+        for det, (p0, p1) in self.det_ranges.items():
+            for field in ("E", "H"):
+                live = self.detector_records(det, field)
+                if live is not None and live.shape[0]:
+                    det._frozen[field].append(live.clone())
+            det._engine = None
+        self.det_ranges = {}
+        self.trace_E = self.trace_H = None
+        self.capacity = self.rec_E = self.rec_H = 0
+
+    def _destroy(self):
+        if self.plan is not None:
+            lib = _native.load()
+            torch.cuda.current_stream().synchronize()
+            lib.fdtd_plan_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self._destroy()
+        except Exception:
+            pass
+
+    def _build(self):
+        g = self.grid
+        lib = _require_gpu(g)
+        self._freeze_traces()
+        self._destroy()
+        keep = []
+        dt = g._dtype
+        d = _native.GridDesc()
+        d.abi_version = _native.ABI_VERSION
+        d.precision = _PRECISION[g.precision]
+        d.nx, d.ny, d.nz = g.Nx, g.Ny, g.Nz
+        d.x_chunk = self.x_chunk
+        d.courant = g.courant_number
+        d.E, d.H = g._E.data_ptr(), g._H.data_ptr()
+        d.E_lo = g._E_lo.data_ptr() if g._E_lo is not None else None
+        d.H_lo = g._H_lo.data_ptr() if g._H_lo is not None else None
+        d.inv_eps = g._inverse_permittivity.data_ptr()
+        d.inv_mu = g._inverse_permeability.data_ptr()
+
+        if len(g.boundaries) > _native.MAX_BOUNDARIES:
+            raise NotImplementedError("more boundaries than the gb300 backend supports")
+        for i, b in enumerate(g.boundaries):
+            bd_ = d.boundaries[i]
+            if isinstance(b, PML):
+                bd_.kind = _native.BOUNDARY_PML
+                bd_.axis, bd_.high, bd_.thickness = b.axis, b.high, b.thickness
+                for name in ("psi_E", "psi_H", "b_E", "c_E", "b_H", "c_H"):
+                    t = getattr(b, name)
+                    if t.dtype != dt or not t.is_contiguous() or t.device.type != "cuda":
+                        raise RuntimeError(f"PML {name} must be a contiguous {dt} CUDA tensor")
+                    setattr(bd_, name, t.data_ptr())
+            elif isinstance(b, PeriodicBoundary):
+                bd_.kind = _native.BOUNDARY_PERIODIC
+                bd_.axis = b.axis
+            else:
+                raise NotImplementedError(f"boundary {type(b).__name__} is not supported by the gb300 backend")
+        d.n_boundaries = len(g.boundaries)
+
+        objs = (_native.ItemDesc * max(1, len(g.objects)))()
+        for i, o in enumerate(g.objects):
+            coefs = o._coefficients(dt)
+            keep.extend(coefs)
+            it = objs[i]
+            it.kind = o._kind
+            it.lo[:] = [o.x.start, o.y.start, o.z.start]
+            it.hi[:] = [o.x.stop, o.y.stop, o.z.stop]
+            for q, c in enumerate(coefs):
+                it.coef[q] = c.data_ptr()
+        d.n_objects = len(g.objects)
+        d.objects = objs
+        keep.append(objs)
+
+        itemsE, itemsH = [], []
+        self.sources = list(g.sources)
+        for col, s in enumerate(self.sources):
+            if not hasattr(s, "_items"):
+                raise NotImplementedError(f"source {type(s).__name__} is not supported by the gb300 backend")
+            for field, kind, comp, lo, hi, w in s._items():
+                it = _native.ItemDesc()
+                it.kind = _native.ITEM_SOFT if kind == "soft" else _native.ITEM_HARD
+                it.comp, it.column, it.source = comp, col, col
+                it.lo[:] = list(lo)
+                it.hi[:] = list(hi)
+                it.weight = w
+                (itemsE if field == "E" else itemsH).append(it)
+        arrE = (_native.ItemDesc * max(1, len(itemsE)))(*itemsE)
+        arrH = (_native.ItemDesc * max(1, len(itemsH)))(*itemsH)
+        d.n_sources_E, d.sources_E = len(itemsE), arrE
+        d.n_sources_H, d.sources_H = len(itemsH), arrH
+        d.n_columns = len(self.sources)
+        keep.extend([arrE, arrH])
+
+        cells = []
+        self.n_probe = 0
+        self.det_ranges = {}
+        self.dfts = []
+        dfts = []
+        nph = 0
+        for det in g.detectors:
+            if isinstance(det, DFTPlaneDetector):
+                dd = _native.DftDesc()
+                dd.lo[:] = [det.x.start, det.y.start, det.z.start]
+                dd.hi[:] = [det.x.stop, det.y.stop, det.z.stop]
+                dd.n_freq = len(det.frequencies)
+                dd.phase_offset = nph
+                dd.acc = det.dft.data_ptr()
+                nph += dd.n_freq
+                dfts.append(dd)
+                self.dfts.append(det)
+            elif hasattr(det, "_probe_cells"):
+                c = det._probe_cells()
+                self.det_ranges[det] = (self.n_probe, self.n_probe + c.size)
+                self.n_probe += c.size
+                cells.append(c)
+                det._engine = self
+            else:
+                raise NotImplementedError(f"detector {type(det).__name__} is not supported by the gb300 backend")
+        if self.n_probe:
+            probe = torch.as_tensor(np.concatenate(cells), dtype=torch.int64, device=g._device)
+            keep.append(probe)
+            d.n_probe_cells, d.probe_cells = self.n_probe, probe.data_ptr()
+        arrD = (_native.DftDesc * max(1, len(dfts)))(*dfts)
+        d.n_dft, d.dft = len(dfts), arrD
+        d.n_phase_columns = nph
+        self.n_phase = nph
+        keep.append(arrD)
+
+        plan = ctypes.c_void_p()
+        _native.check(lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan)), "fdtd_plan_create")
+        self.plan = plan
+        self._keep = keep
+        self.launches_per_step = self.tiling()[5]
+
+    # --- traces ---------------------------------------------------------------
+    def _ensure_capacity(self, need):
+        if need <= self.capacity:
+            return
+        g = self.grid
+        cap = max(need, 2 * self.capacity, 16)
+        newE = torch.empty((cap, self.n_probe, 3), dtype=g._dtype, device=g._device)
+        newH = torch.empty((cap, self.n_probe, 3), dtype=g._dtype, device=g._device)
+        if self.trace_E is not None:
+            newE[: self.rec_E].copy_(self.trace_E[: self.rec_E])
+            newH[: self.rec_H].copy_(self.trace_H[: self.rec_H])
+        self.trace_E, self.trace_H, self.capacity = newE, newH, cap
+
+    def detector_records(self, det, field):
+        rng = self.det_ranges.get(det)
+        buf = self.trace_E if field == "E" else self.trace_H
+        if rng is None or buf is None:
+            return None
+        n = self.rec_E if field == "E" else self.rec_H
+        p0, p1 = rng
+        return buf[:n, p0:p1, :].reshape((n,) + det._rec_shape)
+
+    # --- stepping --------------------------------------------------------------
+    def _tables(self, q0, n):
+        g = self.grid
+        wave = phase = None
+        if self.sources:
+            tab = np.empty((n, len(self.sources)), dtype=np.float64)
+            for c, s in enumerate(self.sources):
+                for r in range(n):
+                    tab[r, c] = s._value(q0 + r)
+            wave = self._wave_stage.upload(tab, g._device)
+        if self.n_phase:
+            ph = np.empty((n, self.n_phase, 2), dtype=np.float64)
+            col = 0
+            for det in self.dfts:
+                for f in det.frequencies:
+                    for r in range(n):
+                        theta = 2.0 * math.pi * f * ((q0 + r) * g.time_step)
+                        ph[r, col, 0] = math.cos(theta)
+                        ph[r, col, 1] = -math.sin(theta)
+                    col += 1
+            phase = self._phase_stage.upload(ph, g._device)
+        return wave, phase
+
+    def _launch(self, n, half):
+        g = self.grid
+        lib = _native.load()
+        q0 = g.time_steps_passed
+        wave, phase = self._tables(q0, n)
+        a = _native.RunArgs()
+        a.n_steps, a.half = n, half
+        a.wave = wave.data_ptr() if wave is not None else None
+        a.phase = phase.data_ptr() if phase is not None else None
+        if self.n_probe:
+            need_E = self.rec_E + (n if half != 2 else 0)
+            need_H = self.rec_H + (n if half != 1 else 0)
+            self._ensure_capacity(max(need_E, need_H))
+            a.trace_E, a.trace_H = self.trace_E.data_ptr(), self.trace_H.data_ptr()
+            a.trace_capacity = self.capacity
+            a.record_E, a.record_H = self.rec_E, self.rec_H
+        stream = torch.cuda.current_stream(g._device).cuda_stream
+        _native.check(lib.fdtd_run(self.plan, ctypes.byref(a), ctypes.c_void_p(stream)), "fdtd_run")
+        if self.n_probe:
+            if half != 2:
+                self.rec_E += n
+            if half != 1:
+                self.rec_H += n
+
+    def run(self, n):
+        """n full steps from time_steps_passed, then time_steps_passed += n."""
+        self.refresh()
+        if n <= 0:
+            return
+        self._launch(n, 0)
+        self.grid.time_steps_passed += n
+
+    def half(self, field):
+        """One E (field='E') or H half step at the current step index."""
+        self.refresh()
+        self._launch(1, 1 if field == "E" else 2)
+
+    def stats(self):
+        lib = _native.load()
+        g = self.grid
+        nbytes = lib.fdtd_stats_scratch_bytes(self.plan)
+        scratch = torch.empty(max(int(nbytes), 8), dtype=torch.uint8, device=g._device)
+        out = torch.empty(5, dtype=torch.float64, device=g._device)
+        stream = torch.cuda.current_stream(g._device).cuda_stream
+        _native.check(lib.fdtd_field_stats(self.plan, out.data_ptr(), scratch.data_ptr(), ctypes.c_void_p(stream)),
+                      "fdtd_field_stats")
+        v = out.cpu().tolist()
+        return {"sum_E2": v[0], "sum_H2": v[1], "max_abs_E": v[2], "max_abs_H": v[3], "nonfinite": int(v[4])}

@@ -1,0 +1,206 @@
+/*
+ * fdtd_gb300.h -- C ABI of the GB300 time-step library for the fdtd FDTD
+ * simulator.
+ *
+ * The reference package (fdtd v0.3.6) is pure Python; its time step is
+ * Grid.update_E / Grid.update_H (fdtd/grid.py:275-325), which call the Yee
+ * curls (fdtd/grid.py:29-76) and the per-component hooks (PML
+ * fdtd/boundaries.py:409-487, periodic copies fdtd/boundaries.py:184-219,
+ * objects fdtd/objects.py:118-277, sources fdtd/sources.py:93-109,278-297,
+ * 476-486, detectors fdtd/detectors.py:114-124,241-265).  This library
+ * replaces that whole chain: one plan describes a registered grid, and each
+ * E or H half step is one fused kernel pass over the grid (plus small plane
+ * kernels where a periodic boundary forces a fixed order).
+ *
+ * Conventions
+ *  - Every pointer inside a descriptor is a DEVICE pointer unless stated.
+ *  - Fields are component-last: element (i, j, k, c) of an (nx, ny, nz, 3)
+ *    array lives at ((i*ny + j)*nz + k)*3 + c.  The element type follows the
+ *    plan precision: float for FDTD_FLOAT32 and FDTD_FLOAT32C, double for
+ *    FDTD_FLOAT64.
+ *  - Functions return an fdtd_status; FDTD_ERR_CUDA keeps the CUDA error code
+ *    for fdtd_last_cuda_error().  Nothing traps or aborts.
+ *  - Stream arguments are cudaStream_t values (0 = legacy default stream).
+ *  - The caller owns every buffer it passes; a plan borrows the pointers in
+ *    its descriptor until fdtd_plan_destroy.  A plan allocates only its own
+ *    small index tables.  Calls on one plan must be serialised by the caller.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_ABI_VERSION 1
+#define FDTD_MAX_BOUNDARIES 9 /* six PML slabs and three periodic axes */
+
+typedef void *fdtd_stream_t; /* a cudaStream_t */
+
+typedef enum {
+    FDTD_OK = 0,
+    FDTD_ERR_ARGUMENT = 1,    /* bad descriptor, size or pointer */
+    FDTD_ERR_UNSUPPORTED = 2, /* valid input this library does not handle */
+    FDTD_ERR_CUDA = 3,        /* a CUDA call failed, see fdtd_last_cuda_error */
+    FDTD_ERR_NONFINITE = 4,   /* a field holds NaN or Inf */
+    FDTD_ERR_RANGE = 5        /* a record or size is out of range */
+} fdtd_status;
+
+typedef enum {
+    FDTD_FLOAT32 = 0,  /* float fields and arithmetic */
+    FDTD_FLOAT32C = 1, /* float fields plus a float compensation term per
+                          E/H value (two-float accumulation) */
+    FDTD_FLOAT64 = 2   /* double, same operation order as the reference */
+} fdtd_precision;
+
+typedef enum { FDTD_BOUNDARY_PML = 0, FDTD_BOUNDARY_PERIODIC = 1 } fdtd_boundary_kind;
+
+/* One entry of grid.boundaries, in registration order.
+ * PML slab: replaces PML.update_phi_E/H and PML.update_E/H
+ * (fdtd/boundaries.py:409-487) for the slab subclasses of
+ * fdtd/boundaries.py:490-625.  Only the two auxiliaries per half step that
+ * can be non-zero are stored (compact layout): psi_E holds, for every slab
+ * cell, the pair (psi driving E[(axis+1)%3], psi driving E[(axis+2)%3]); the
+ * slab cells are ordered like the grid with the slab axis cut to `thickness`.
+ * Periodic: replaces _PeriodicBoundary{X,Y,Z}.update_E/H
+ * (fdtd/boundaries.py:184-219). */
+typedef struct {
+    int32_t kind;       /* fdtd_boundary_kind */
+    int32_t axis;       /* 0 = x, 1 = y, 2 = z */
+    int32_t high;       /* PML: 0 = low side, 1 = high side */
+    int32_t thickness;  /* PML: cells along axis */
+    void *psi_E;        /* PML: [slab cells][2] */
+    void *psi_H;        /* PML: [slab cells][2] */
+    const void *b_E;    /* PML: [thickness] exp(-(sigma_E/k + a) * courant) */
+    const void *c_E;    /* PML: [thickness] */
+    const void *b_H;    /* PML: [thickness] */
+    const void *c_H;    /* PML: [thickness] */
+} fdtd_boundary_desc;
+
+typedef enum {
+    FDTD_ITEM_OBJECT = 0,      /* E += coef0 * curlH; coef0 = courant * inverse_permittivity
+                                  (fdtd/objects.py:118-129) */
+    FDTD_ITEM_ABSORBING = 1,   /* E = E*coef0 + (coef1*curlH)/coef2 with coef0 = (1-f)/(1+f),
+                                  coef1 = courant*inverse_permittivity, coef2 = 1+f
+                                  (fdtd/objects.py:207-221); float plans use coef1/coef2
+                                  premultiplied in coef1 and ignore coef2 */
+    FDTD_ITEM_ANISOTROPIC = 2, /* E += courant * (coef0 @ curlH), coef0 [cell][3][3]
+                                  (fdtd/objects.py:254-269) */
+    FDTD_ITEM_SOFT = 3,        /* F[comp] += weight * wave[column] (PointSource, LineSource) */
+    FDTD_ITEM_HARD = 4         /* F[comp]  = weight * wave[column] (PlaneSource) */
+} fdtd_item_kind;
+
+/* An object box or a source box/point.  Object coefficient arrays are
+ * box-local: cell (i, j, k) of the box is entry ((i*bny + j)*bnz + k). */
+typedef struct {
+    int32_t kind;     /* fdtd_item_kind */
+    int32_t comp;     /* sources: field component 0..2 */
+    int32_t column;   /* sources: column of the per-step waveform row */
+    int32_t source;   /* sources: index in grid.sources (fixes the order) */
+    int32_t lo[3];    /* first cell (x, y, z) */
+    int32_t hi[3];    /* one past the last cell (x, y, z) */
+    double weight;    /* sources: amplitude or profile weight */
+    const void *coef[3];
+} fdtd_item_desc;
+
+/* Running DFT of E on a box: acc[f][cell][c] += E[cell][c] * (phase_re + i*phase_im),
+ * accumulated in double after every E half step (not in the reference). */
+typedef struct {
+    int32_t lo[3];
+    int32_t hi[3];
+    int32_t n_freq;
+    int32_t phase_offset; /* first frequency column of the per-step phase row */
+    double *acc;          /* [n_freq][box cells][3] interleaved (re, im) */
+} fdtd_dft_desc;
+
+typedef struct {
+    int32_t abi_version;  /* FDTD_ABI_VERSION */
+    int32_t precision;    /* fdtd_precision */
+    int32_t nx, ny, nz;
+    int32_t x_chunk;      /* cells per CTA along x; 0 = automatic */
+    double courant;
+    void *E;              /* [nx][ny][nz][3] */
+    void *H;
+    void *E_lo;           /* FDTD_FLOAT32C: compensation terms, else NULL */
+    void *H_lo;
+    const void *inv_eps;  /* [nx][ny][nz][3] grid.inverse_permittivity */
+    const void *inv_mu;   /* [nx][ny][nz][3] grid.inverse_permeability */
+    int32_t n_boundaries;
+    fdtd_boundary_desc boundaries[FDTD_MAX_BOUNDARIES];
+    int32_t n_objects;    /* grid.objects, registration order */
+    const fdtd_item_desc *objects;    /* HOST array */
+    int32_t n_sources_E;  /* source items acting in the E half step, grid.sources order */
+    const fdtd_item_desc *sources_E;  /* HOST array */
+    int32_t n_sources_H;
+    const fdtd_item_desc *sources_H;  /* HOST array */
+    int32_t n_columns;    /* width of one waveform row */
+    int32_t n_probe_cells;            /* detector sample points, all detectors */
+    const int64_t *probe_cells;       /* [n_probe_cells] linear cell index */
+    int32_t n_dft;
+    const fdtd_dft_desc *dft;         /* HOST array */
+    int32_t n_phase_columns;          /* width of one DFT phase row (pairs) */
+} fdtd_grid_desc;
+
+typedef struct fdtd_plan fdtd_plan;
+
+/* Arguments of one fdtd_run call: n_steps full steps, or a single half step. */
+typedef struct {
+    int64_t n_steps;
+    int32_t half;          /* 0: full steps; 1: only the E half; 2: only the H half (n_steps = 1) */
+    int32_t reserved;
+    const double *wave;    /* [n_steps][n_columns] waveform value per source column, step s */
+    const double *phase;   /* [n_steps][n_phase_columns][2] DFT factors (cos, -sin) */
+    void *trace_E;         /* [capacity][n_probe_cells][3] detector samples after E halves */
+    void *trace_H;         /* [capacity][n_probe_cells][3] after H halves */
+    int64_t trace_capacity;
+    int64_t record_E;      /* row of trace_E written by the first E half */
+    int64_t record_H;
+} fdtd_run_args;
+
+/* Build a plan for a registered grid (replaces the per-step dispatch of
+ * fdtd/grid.py:275-325).  Validates the descriptor, chooses the launch
+ * tiling and builds the per-CTA object and source lists. */
+int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out);
+
+/* Release the plan's own tables (never the caller's buffers). */
+int fdtd_plan_destroy(fdtd_plan *plan);
+
+/* Grid.run / Grid.step / Grid.update_E / Grid.update_H
+ * (fdtd/grid.py:250-325): n_steps steps (or one half step) with detector
+ * sampling and DFT accumulation after each half step. */
+int fdtd_run(fdtd_plan *plan, const fdtd_run_args *args, fdtd_stream_t stream);
+
+/* curl_E (fdtd/grid.py:29-51) and curl_H (fdtd/grid.py:54-76) as
+ * stand-alone kernels: out = curl(in), both [nx][ny][nz][3]. */
+int fdtd_curl_E(int32_t precision, const void *E, void *out, int32_t nx, int32_t ny, int32_t nz,
+                fdtd_stream_t stream);
+int fdtd_curl_H(int32_t precision, const void *H, void *out, int32_t nx, int32_t ny, int32_t nz,
+                fdtd_stream_t stream);
+
+/* Field statistics for failure detection (no reference counterpart; the
+ * reference has no health check): stats[0] = sum E^2, stats[1] = sum H^2,
+ * stats[2] = max |E|, stats[3] = max |H|, stats[4] = number of non-finite
+ * values, written to the DEVICE array `stats` (5 doubles).  Uses `scratch`,
+ * a device buffer of fdtd_stats_scratch_bytes(plan) bytes.  Returns
+ * FDTD_OK; the caller reads stats[4] to decide. */
+size_t fdtd_stats_scratch_bytes(const fdtd_plan *plan);
+int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_stream_t stream);
+
+/* Launch tiling chosen by the plan: out[0..5] = cells per thread along z,
+ * threads along z, rows along y, cells along x per CTA, CTAs, kernels per
+ * full step. */
+int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out6);
+
+const char *fdtd_status_string(int32_t status);
+int32_t fdtd_last_cuda_error(void);
+/* sizeof of the ABI structs, for binding checks: 0 grid_desc, 1 boundary_desc,
+ * 2 item_desc, 3 dft_desc, 4 run_args. */
+size_t fdtd_abi_sizeof(int32_t which);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDTD_GB300_H */

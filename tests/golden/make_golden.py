@@ -1,0 +1,58 @@
+"""Generate the golden fixtures by running the reference fdtd package (numpy backend).
+
+Usage (needs a checkout of the reference; nothing else in the repository reads it):
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference imports matplotlib for plotting only; a no-op stand-in from
+``tests/golden/mplstub`` is put on ``sys.path`` first.  Outputs:
+
+* ``ref_curls.npz`` -- curl_E / curl_H of the reference applied to the inputs of
+  its own known-answer tests (tests/test_grid.py:47-164 use
+  ``RandomState(0).randn(3,3,3,3)`` and ``RandomState(1).randn(3,3,3,3)``).
+* ``ref_<scene>.npz`` -- final E, H and every detector trace for each scene of
+  ``golden_scenes.SCENES`` after its stated number of steps.
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def load_reference(path):
+    sys.path.insert(0, os.path.join(HERE, "mplstub"))
+    sys.path.insert(0, path)
+    import fdtd  # noqa: E402  (the reference package)
+    import fdtd.boundaries
+
+    fdtd.set_backend("numpy")
+    fdtd.DomainBorderPML = fdtd.boundaries.DomainBorderPML
+    return fdtd
+
+
+def main(ref_path):
+    fdtd = load_reference(ref_path)
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, HERE)
+    import golden_scenes
+    from fdtd.grid import curl_E, curl_H
+
+    E0 = np.random.RandomState(0).randn(3, 3, 3, 3)
+    H1 = np.random.RandomState(1).randn(3, 3, 3, 3)
+    np.savez(os.path.join(HERE, "ref_curls.npz"), E=E0, curl_E=curl_E(E0), H=H1, curl_H=curl_H(H1),
+             reference_version=fdtd.__version__)
+    for name, build in golden_scenes.SCENES.items():
+        grid, steps, drive = build(fdtd)
+        drive(grid, steps)
+        snap = golden_scenes.snapshot(grid)
+        snap["steps"] = np.array(steps)
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **snap)
+        print(name, {k: v.shape for k, v in snap.items()})
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,227 @@
+"""Parity of the CUDA time step (through the C ABI) with the reference.
+
+* float64 plans against the golden fixtures made by the reference itself:
+  relative L2 <= 1e-12 on E, H and every detector trace (the spec bar).
+* float32 and compensated float32 plans against the same fixtures: <= 1e-4.
+* larger seeded scenes against the CPU oracle run in-process, with the same
+  tolerances, covering every config generator (c1..c5) at reduced size.
+* edge behaviour: run/step/half-step equivalence, tiling invariance, plan
+  rebuilds, stand-alone curls on the reference's known-answer inputs.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import golden_scenes
+from helpers import rel_l2, to_np
+from oracle import fdtd_oracle as fo
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-12   # float64: relative L2 against the reference numpy float64 backend
+TOL32 = 1e-4    # float32 / float32c: relative L2 of detector traces and fields
+
+
+@pytest.fixture(scope="module", autouse=True)
+def native():
+    from fdtd_gb300 import _native
+
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return _native.load()
+
+
+def _compare(snap, ref, tol, label):
+    worst = 0.0
+    for key in ref.files:
+        if key in ("steps",):
+            continue
+        a, b = snap[key], ref[key]
+        assert a.shape == b.shape, f"{label}:{key} shape {a.shape} vs {b.shape}"
+        if key == "q":
+            assert int(a) == int(b)
+            continue
+        err = rel_l2(a, b)
+        worst = max(worst, err)
+        assert err <= tol, f"{label}:{key} relative L2 {err:.3e} > {tol:.0e}"
+    return worst
+
+
+@pytest.mark.parametrize("name", sorted(golden_scenes.SCENES))
+def test_float64_matches_reference_golden(fd, name):
+    fd.set_backend("gb300.float64")
+    grid, steps, drive = golden_scenes.SCENES[name](fd)
+    drive(grid, steps)
+    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    _compare(golden_scenes.snapshot(grid), ref, TOL64, name)
+
+
+@pytest.mark.parametrize("prec", ["float32", "float32c"])
+@pytest.mark.parametrize("name", sorted(golden_scenes.SCENES))
+def test_float32_close_to_reference_golden(fd, prec, name):
+    fd.set_backend("gb300." + prec)
+    grid, steps, drive = golden_scenes.SCENES[name](fd)
+    drive(grid, steps)
+    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    _compare(golden_scenes.snapshot(grid), ref, TOL32, f"{name}/{prec}")
+
+
+def _curl_via_abi(native, fn, arr, precision, dtype):
+    t = torch.as_tensor(arr, dtype=dtype, device="cuda").contiguous()
+    out = torch.empty_like(t)
+    nx, ny, nz, _ = t.shape
+    rc = fn(precision, t.data_ptr(), out.data_ptr(), nx, ny, nz, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_curls_on_reference_known_answers(native):
+    d = np.load(os.path.join(GOLDEN, "ref_curls.npz"))
+    assert np.array_equal(_curl_via_abi(native, native.fdtd_curl_E, d["E"], 2, torch.float64), d["curl_E"])
+    assert np.array_equal(_curl_via_abi(native, native.fdtd_curl_H, d["H"], 2, torch.float64), d["curl_H"])
+    c32 = _curl_via_abi(native, native.fdtd_curl_E, d["E"], 0, torch.float32)
+    assert np.allclose(c32, d["curl_E"], rtol=1e-5, atol=1e-5)
+
+
+def test_curls_random_against_oracle(native):
+    rng = np.random.default_rng(7)
+    for shape in [(5, 7, 9, 3), (16, 4, 32, 3), (1, 6, 1, 3)]:
+        a = rng.standard_normal(shape)
+        assert np.array_equal(_curl_via_abi(native, native.fdtd_curl_E, a, 2, torch.float64), fo.curl_E(a))
+        assert np.array_equal(_curl_via_abi(native, native.fdtd_curl_H, a, 2, torch.float64), fo.curl_H(a))
+
+
+SCENES = {
+    "c1_n32": (lambda fd: fo_scene(fd, "c1", n=32, pml=6), 60),
+    "c2_n24": (lambda fd: fo_scene(fd, "c2", n=24, pml=4), 50),
+    "c3_n32_periodic_last": (lambda fd: fo_scene(fd, "c3", n=32, pml=5), 50),
+    "c3_n32_periodic_first": (lambda fd: fo_scene(fd, "c3", n=32, pml=5, periodic_first=True), 50),
+    "c4_n32": (lambda fd: fo_scene(fd, "c4", n=32, pml=4, d=12), 50),
+    "c5_small": (lambda fd: fo_scene(fd, "c5", nx=32, ny=28, nz=24, pml=4), 60),
+}
+
+
+def fo_scene(fd, which, **kw):
+    from fdtd_gb300 import scenes
+
+    return getattr(scenes, which)(fd, **kw)
+
+
+def _run_both(fd, prec, key):
+    build, steps = SCENES[key]
+    fd.set_backend("gb300." + prec)
+    g = build(fd)
+    g.run(steps, progress_bar=False)
+    o = build(fo)
+    o.run(steps)
+    return g, o
+
+
+def _dft_or_records(det):
+    if hasattr(det, "dft"):
+        return to_np(det.dft.real), to_np(det.dft.imag)
+    return (np.asarray(det.E), np.asarray(det.H))
+
+
+@pytest.mark.parametrize("key", sorted(SCENES))
+@pytest.mark.parametrize("prec,tol", [("float64", TOL64), ("float32", TOL32), ("float32c", TOL32)])
+def test_scenes_against_oracle(fd, key, prec, tol):
+    g, o = _run_both(fd, prec, key)
+    assert rel_l2(g.E, o.E) <= tol
+    assert rel_l2(g.H, o.H) <= tol
+    assert len(g.detectors) == len(o.detectors)
+    for det, odet in zip(g.detectors, o.detectors):
+        mine, theirs = _dft_or_records(det), _dft_or_records(odet)
+        for a, b in zip(mine, theirs):
+            assert a.shape == np.asarray(b).shape
+            assert rel_l2(a, b) <= tol, f"{key}/{prec} {type(det).__name__}"
+
+
+def test_run_step_and_halves_agree(fd):
+    fd.set_backend("gb300.float64")
+    build, _ = SCENES["c1_n32"]
+    a, b, c = build(fd), build(fd), build(fd)
+    a.run(12, progress_bar=False)
+    for _ in range(12):
+        b.step()
+    for _ in range(12):
+        c.update_E()
+        c.update_H()
+        c.time_steps_passed += 1
+    for g in (b, c):
+        assert torch.equal(a.E, g.E) and torch.equal(a.H, g.H)
+        assert np.array_equal(np.asarray(a.detector.E), np.asarray(g.detector.E))
+
+
+@pytest.mark.parametrize("prec", ["float64", "float32", "float32c"])
+def test_tiling_does_not_change_results(fd, prec):
+    fd.set_backend("gb300." + prec)
+    build, _ = SCENES["c2_n24"]
+    ref = build(fd)
+    ref.run(20, progress_bar=False)
+    for chunk in (1, 3, 7, 24):
+        g = build(fd)
+        g._ensure_engine().set_x_chunk(chunk)
+        g.run(20, progress_bar=False)
+        assert torch.equal(g.E, ref.E) and torch.equal(g.H, ref.H), chunk
+
+
+def test_records_survive_plan_rebuild(fd):
+    fd.set_backend("gb300.float64")
+    build, _ = SCENES["c1_n32"]
+    g, o = build(fd), build(fo)
+    g.run(5, progress_bar=False)
+    o.run(5)
+    g[:, 3, 3] = fd.LineDetector(name="late")
+    o[:, 3, 3] = fo.LineDetector(name="late")
+    g.run(6, progress_bar=False)
+    o.run(6)
+    assert len(g.detector.E) == 11 and len(g.late.E) == 6
+    assert rel_l2(np.asarray(g.detector.E), np.stack(o.detector.E)) <= TOL64
+    assert rel_l2(np.asarray(g.late.H), np.stack(o.late.H)) <= TOL64
+
+
+def test_object_change_between_runs(fd):
+    """Assigning an object's inverse permittivity rebuilds its coefficients."""
+    fd.set_backend("gb300.float64")
+    build, _ = SCENES["c4_n32"]
+    g, o = build(fd), build(fo)
+    g.run(10, progress_bar=False)
+    o.run(10)
+    new = np.full(o.objects[0].inverse_permittivity.shape, 0.3)
+    g.objects[0].inverse_permittivity = new
+    o.objects[0].inverse_permittivity = new.copy()
+    g.run(10, progress_bar=False)
+    o.run(10)
+    assert rel_l2(g.E, o.E) <= TOL64
+
+
+def test_field_stats_detects_nonfinite(fd):
+    fd.set_backend("gb300.float32")
+    build, _ = SCENES["c1_n32"]
+    g = build(fd)
+    g.run(10, progress_bar=False)
+    s = g.field_stats()
+    e = g.E.double()
+    assert s["nonfinite"] == 0
+    assert s["sum_E2"] == pytest.approx(float((e * e).sum()), rel=1e-6)
+    assert s["max_abs_E"] == pytest.approx(float(e.abs().max()), rel=1e-7)
+    g.E[3, 4, 5, 1] = float("nan")
+    g.H[1, 1, 1, 0] = float("inf")
+    assert g.field_stats()["nonfinite"] == 2
+
+
+def test_reset_keeps_plan(fd):
+    fd.set_backend("gb300.float64")
+    build, _ = SCENES["c1_n32"]
+    g = build(fd)
+    g.run(5, progress_bar=False)
+    g.reset()
+    assert g.time_steps_passed == 0 and float(g.E.abs().max()) == 0.0
+    g.run(3, progress_bar=False)
+    assert float(g.E.abs().max()) > 0.0
