@@ -1,0 +1,447 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 fdtd time step.
+
+Workload: config 3 -- a 768^3 grid with 400 random dielectric blocks
+(eps in {1, 2.25, 12.1}, seed 3) rasterised into the grid permittivity,
+20-cell PML on y and z, periodic x, a point source at the centre and a line
+detector along x through the centre.  A step is one full E + H time step of
+the whole grid.  Fields and materials (about 22 GB in float32) are larger
+than L2, so no flush is needed between steps.
+
+Printed line (rank 0): value = float32 Gcell-updates/s of all ranks, with
+the float64 and compensated float32 runs of the same grid, the float32 /
+float64 detector-trace error, the roofline of the fused half-step kernels
+(HBM-bound), the CPU oracle on a crop of the same generator, the end-to-end
+figure through the public API with per-step host<->device copies, launch
+count and SM clocks sampled during the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+numpy oracle port of fdtd's time step) on a crop of the same workload.
+N > 1 runs one independent replica per rank (the path has no exchange step).
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from datetime import datetime
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s FP32 vs FP64 at stated error; %HBM peak; adjoint/forward time"
+UNIT = "Gcell-updates/s"
+# algorithmic bytes per cell and half step: read field, read neighbour field,
+# read inverse material, write field (3 components each); compensated adds the
+# read and write of the compensation term.  PML slab cells add the read and
+# write of their two auxiliaries.
+CELL_BYTES = {"float32": 48, "float32c": 72, "float64": 96}
+SLAB_BYTES = {"float32": 16, "float32c": 16, "float64": 32}
+
+
+def parse():
+    p = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--n", type=int, default=768, help="grid edge (config 3 is 768)")
+    p.add_argument("--x-chunk", type=int, default=0, help="planes per CTA along x (0 = plan default)")
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
+    p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--only", choices=["float32", "float32c", "float64"], default=None)
+    return p.parse_args()
+
+
+# --------------------------------------------------------------------------
+# distributed helpers (replicas only)
+# --------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        import torch
+
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg is not None:
+            self.pg.barrier()
+
+    def max(self, v):
+        if self.pg is None:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg is not None:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self, t0, t1):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                ts = datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                continue
+            rows.append((ts, parts))
+        os.unlink(self.path)
+        inside = [p for ts, p in rows if t0 - 0.15 <= ts <= t1 + 0.15] or [p for _, p in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        sm, smax, power = [], [], []
+        for p in inside:
+            try:
+                sm.append(float(p[2]))
+                smax.append(float(p[3]))
+                power.append(float(p[4]))
+            except ValueError:
+                pass
+            for k, name in enumerate(names):
+                if p[6 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(inside),
+                "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile(precision, n):
+    """DRAM bytes per fused-kernel launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    ent = d.get(precision)
+    if not ent:
+        return None
+    # per-cell traffic measured on a smaller grid, scaled to this workload
+    return ent["bytes_per_cell"] * n ** 3
+
+
+def build_grid(fd, scenes, prec, n, eps, x_chunk):
+    fd.set_backend("gb300." + prec)
+    pml = max(2, int(round(20 * n / 768)))
+    g = scenes.c3(fd, n=n, pml=pml, eps=eps, detector=True)
+    eng = g._ensure_engine()
+    if x_chunk:
+        eng.set_x_chunk(x_chunk)
+    return g, eng
+
+
+def slab_cells(grid):
+    from fdtd_gb300 import PML
+
+    tot = 0
+    for b in grid.boundaries:
+        if isinstance(b, PML):
+            tot += b.shape[0] * b.shape[1] * b.shape[2]
+    return tot
+
+
+def run_precision(prec, args, dist, fd, scenes, eps, want_halves, want_e2e, sampler=None):
+    import torch
+
+    n = args.n
+    cells = n ** 3
+    g, eng = build_grid(fd, scenes, prec, n, eps, args.x_chunk)
+    tiling = eng.tiling()
+    g.run(args.warmup, progress_bar=False)
+    torch.cuda.synchronize()
+    dist.barrier()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if sampler is not None:
+        sampler.start()
+    t0 = time.time()
+    ev0.record(stream)
+    g.run(args.steps, progress_bar=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t1 = time.time()
+    dist.barrier()
+    ms = dist.max(ev0.elapsed_time(ev1))
+    clocks = sampler.stop(t0, t1) if sampler is not None else None
+    out = {
+        "precision": prec,
+        "ms_per_step": ms / args.steps,
+        "gcells": cells * args.steps * dist.world / (ms * 1e-3) / 1e9,
+        "launches_per_step": int(tiling[5]),
+        "tiling": {"cells_per_thread_z": int(tiling[0]), "threads_z": int(tiling[1]), "rows_y": int(tiling[2]),
+                   "planes_x": int(tiling[3]), "ctas": int(tiling[4])},
+        "clocks": clocks,
+        "trace": g.detector.E.tensor()[: args.warmup + args.steps].double().cpu(),
+        "stats": g.field_stats(),
+    }
+    algo = cells * CELL_BYTES[prec] + slab_cells(g) * SLAB_BYTES[prec]
+    out["algo_bytes_half"] = algo
+    if want_halves:
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for a, b, c in evs:
+            a.record(stream)
+            g.update_E()
+            b.record(stream)
+            g.update_H()
+            c.record(stream)
+            g.time_steps_passed += 1
+        torch.cuda.synchronize()
+        tE = [a.elapsed_time(b) for a, b, c in evs]
+        tH = [b.elapsed_time(c) for a, b, c in evs]
+        out["half_ms"] = {"E": statistics.mean(tE), "H": statistics.mean(tH)}
+    if want_e2e:
+        m = g.detector._rec_shape
+        host = torch.empty((args.steps,) + m, dtype=g.E.dtype).pin_memory()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for s in range(args.steps):
+            g.step()
+            host[s].copy_(g.detector.E[-1], non_blocking=True)
+        torch.cuda.synchronize()
+        w1 = time.perf_counter()
+        e2e_s = dist.max(w1 - w0)
+        out["e2e"] = {"value": cells * args.steps * dist.world / e2e_s / 1e9, "unit": UNIT,
+                      "h2d_bytes_per_step": 8 * len(g.sources),
+                      "d2h_bytes_per_step": int(host[0].numel() * host.element_size()),
+                      "how": "per step: grid.step() (host waveform -> pinned -> device, fused kernels via the "
+                             "C ABI) then the step's detector record copied device -> pinned host"}
+    del g, eng
+    torch.cuda.empty_cache()
+    return out
+
+
+def cpu_oracle_rate(budget_s, n_full):
+    """Time the numpy oracle (one core) on a crop of the config-3 generator."""
+    from fdtd_gb300 import scenes
+    from oracle import fdtd_oracle as fo
+
+    n = 96
+    g = scenes.c3(fo, n=n, pml=3, detector=True)
+    g.step()
+    t0 = time.perf_counter()
+    g.step()
+    per = time.perf_counter() - t0
+    steps = int(max(3, min(60, budget_s / max(per, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.step()
+    dt = time.perf_counter() - t0
+    return {"value": n ** 3 * steps / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"numpy float64 oracle of fdtd's time step on the config-3 generator cropped to {n}^3 "
+                      f"(3-cell PML, periodic x, point source, line detector), {steps} steps, "
+                      f"{dt:.1f} s, one host core (numpy elementwise is single-threaded)"}
+
+
+def gb300_arm(args):
+    import torch
+
+    import fdtd_gb300 as fd
+    from fdtd_gb300 import scenes
+
+    dist = Dist()
+    if torch.cuda.is_available():
+        torch.cuda.set_device(dist.local)
+    n = args.n
+    eps = scenes.c3_permittivity(n, device="cuda")
+    precs = [args.only] if args.only else ["float32", "float64", "float32c"]
+    res = {}
+    for prec in precs:
+        sampler = ClockSampler(dist.local) if prec == precs[0] else None
+        res[prec] = run_precision(prec, args, dist, fd, scenes, eps, want_halves=prec != "float32c",
+                                  want_e2e=prec == precs[0], sampler=sampler)
+    del eps
+    main = res[precs[0]]
+    peak, peak_kind = peaks()
+    kern = max(main["half_ms"], key=main["half_ms"].get) if "half_ms" in main else "E"
+    t_kern = main["half_ms"][kern] if "half_ms" in main else main["ms_per_step"] / 2
+    achieved = main["algo_bytes_half"] / (t_kern * 1e-3) / 1e9
+    traffic = traffic_from_profile(precs[0], n)
+    line = {
+        "metric": METRIC,
+        "value": main["gcells"],
+        "unit": UNIT,
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": main["ms_per_step"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"float32": "f32", "float32c": "f32 (compensated)", "float64": "f64"}[precs[0]],
+        "data": "synthetic: config-3 generator (seed 3), zero initial fields",
+        "config": {
+            "workload": f"config3_{n}^3_{precs[0]}",
+            "grid": [n, n, n],
+            "geometry": "400 random blocks eps in {1,2.25,12.1}, PML y/z, periodic x, centre point source, "
+                        "line detector",
+            "l2": "inputs larger than L2 (fields + materials >= 22 GB at 768^3); no flush",
+            "parallelism": "replicas" if dist.world > 1 else "single GPU",
+        },
+        "roofline": {
+            "bound": "hbm",
+            "kernel": f"k_update_{kern} ({precs[0]}, fused {kern} half step incl. its small epilogue kernels)",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "peak_kind": f"{peak_kind} (STREAM-style copy, MEASURED_PEAKS.json hbm_gbs)",
+            "algo_bytes_per_launch": main["algo_bytes_half"],
+            "traffic": traffic,
+        },
+        "gpu_launches": main["launches_per_step"] * args.steps,
+        "clocks": main["clocks"],
+        "e2e": main.get("e2e"),
+        "tiling": main["tiling"],
+    }
+    if "float64" in res:
+        f64 = res["float64"]
+        line["fp64"] = {"value": f64["gcells"], "ms_per_step": f64["ms_per_step"],
+                        "hbm_frac": (f64["algo_bytes_half"] / (max(f64["half_ms"].values()) * 1e-3) / 1e9) / peak
+                        if "half_ms" in f64 else None}
+        if precs[0] == "float32":
+            line["fp32_over_fp64"] = main["gcells"] / f64["gcells"]
+        ref = f64["trace"]
+        errs = {}
+        for prec in ("float32", "float32c"):
+            if prec in res:
+                tr = res[prec]["trace"]
+                errs[prec] = float((tr - ref).norm() / ref.norm())
+        line["error"] = {"trace_rel_l2_vs_fp64": errs, "records": int(ref.shape[0]),
+                         "detector": "line along x through the source"}
+    if "float32c" in res:
+        line["fp32c"] = {"value": res["float32c"]["gcells"], "ms_per_step": res["float32c"]["ms_per_step"]}
+    line["nonfinite"] = {p: r["stats"]["nonfinite"] for p, r in res.items()}
+    if dist.rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_oracle_rate(args.cpu_seconds, n)
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+# --------------------------------------------------------------------------
+# reference arm: the CPU implementation of the algorithm (numpy oracle port)
+# --------------------------------------------------------------------------
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from fdtd_gb300 import scenes
+    from oracle import fdtd_oracle as fo
+
+    # crop of the config-3 generator sized so that warmup + steps fit about two minutes
+    g = scenes.c3(fo, n=48, pml=2, detector=True)
+    t0 = time.perf_counter()
+    g.step()
+    rate = 48 ** 3 / max(time.perf_counter() - t0, 1e-4)
+    budget = 120.0
+    n = int((rate * budget / max(1, args.steps + args.warmup)) ** (1.0 / 3.0))
+    n = max(24, min(args.n, 160, n))
+    pml = max(2, int(round(20 * n / 768)))
+    g = scenes.c3(fo, n=n, pml=pml, detector=True)
+    for _ in range(args.warmup):
+        g.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.step()
+    dt = time.perf_counter() - t0
+    value = n ** 3 * args.steps / dt / 1e9
+    sample = (f"numpy float64 oracle (port of fdtd's numpy time step) on the config-3 generator cropped to "
+              f"{n}^3 ({pml}-cell PML, periodic x, point source, line detector); one host core")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: config-3 generator (seed 3), zero initial fields",
+        "config": {"workload": f"config3_{args.n}^3_float32", "sample_grid": [n, n, n],
+                   "parallelism": "single host process"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gb300_arm(args)
+
+
+if __name__ == "__main__":
+    main()

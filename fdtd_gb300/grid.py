@@ -67,11 +67,13 @@ class Grid:
         divided in float64 then stored in the grid precision."""
         shp = (self.Nx, self.Ny, self.Nz, 3)
         if torch.is_tensor(value) or isinstance(value, np.ndarray):
-            t = torch.as_tensor(np.asarray(value.detach().cpu()) if torch.is_tensor(value) else value,
-                                dtype=torch.float64).to(self._device)
+            if torch.is_tensor(value):
+                t = value.detach().to(device=self._device, dtype=torch.float64)
+            else:
+                t = torch.as_tensor(value, dtype=torch.float64).to(self._device)
             if t.ndim == 3:
                 t = t[:, :, :, None]
-            inv = torch.ones(shp, dtype=torch.float64, device=self._device) / t
+            inv = torch.broadcast_to(1.0 / t, shp)
         else:
             inv = torch.full(shp, 1.0 / float(value), dtype=torch.float64, device=self._device)
         return inv.to(self._dtype).contiguous()

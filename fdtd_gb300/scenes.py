@@ -79,22 +79,30 @@ def c2(fd, n=256, pml=16, seed=2, conductivity=1e4, eps=None):
     return grid
 
 
-def c3_permittivity(n, seed=3, nblocks=400):
-    """400 random axis-aligned blocks rasterised in seed order (last writer wins)."""
+def c3_permittivity(n, seed=3, nblocks=400, device=None):
+    """400 random axis-aligned blocks rasterised in seed order (last writer wins).
+
+    With ``device`` the (n, n, n) float64 array is a torch tensor built on that
+    device (same values; avoids a multi-GB host array at full size)."""
     rng = np.random.default_rng(seed)
-    eps = np.ones((n, n, n), dtype=np.float64)
+    if device is not None:
+        import torch
+
+        eps = torch.ones((n, n, n), dtype=torch.float64, device=device)
+    else:
+        eps = np.ones((n, n, n), dtype=np.float64)
     values = np.array([1.0, 2.25, 12.1])
     for _ in range(nblocks):
         edges = rng.integers(8, 65, size=3)
         edges = np.maximum(2, np.rint(edges * n / 768.0)).astype(int)
         origin = [int(rng.integers(0, n - e + 1)) for e in edges]
-        val = values[int(rng.integers(0, 3))]
+        val = float(values[int(rng.integers(0, 3))])
         eps[origin[0]:origin[0] + edges[0], origin[1]:origin[1] + edges[1],
             origin[2]:origin[2] + edges[2]] = val
     return eps
 
 
-def c3(fd, n=768, pml=20, seed=3, periodic_first=False, eps=None):
+def c3(fd, n=768, pml=20, seed=3, periodic_first=False, eps=None, detector=False):
     if eps is None:
         eps = c3_permittivity(n, seed)
     grid = fd.Grid((n, n, n), grid_spacing=SPACING, permittivity=eps, permeability=1.0)
@@ -108,6 +116,8 @@ def c3(fd, n=768, pml=20, seed=3, periodic_first=False, eps=None):
         grid[0, :, :] = fd.PeriodicBoundary(name="xbounds")
     c = n // 2
     grid[c, c, c] = fd.PointSource(period=WAVELENGTH / C0, name="source")
+    if detector:
+        grid[:, c, c] = fd.LineDetector(name="detector")
     return grid
 
 
