@@ -23,6 +23,7 @@ N > 1 runs one independent replica per rank (the path has no exchange step).
 """
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -54,6 +55,9 @@ def parse():
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--n", type=int, default=768, help="grid edge (config 3 is 768)")
     p.add_argument("--x-chunk", type=int, default=0, help="planes per CTA along x (0 = plan default)")
+    p.add_argument("--variant", type=int, default=0, help="0 auto, 1 register streaming, 2 TMA-staged")
+    p.add_argument("--tile-rows", type=int, default=0)
+    p.add_argument("--stages", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--only", choices=["float32", "float32c", "float64"], default=None)
@@ -184,13 +188,12 @@ def traffic_from_profile(precision, n):
     return ent["bytes_per_cell"] * n ** 3
 
 
-def build_grid(fd, scenes, prec, n, eps, x_chunk):
+def build_grid(fd, scenes, prec, n, eps, args):
     fd.set_backend("gb300." + prec)
     pml = max(2, int(round(20 * n / 768)))
     g = scenes.c3(fd, n=n, pml=pml, eps=eps, detector=True)
     eng = g._ensure_engine()
-    if x_chunk:
-        eng.set_x_chunk(x_chunk)
+    eng.set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages, x_chunk=args.x_chunk)
     return g, eng
 
 
@@ -209,7 +212,7 @@ def run_precision(prec, args, dist, fd, scenes, eps, want_halves, want_e2e, samp
 
     n = args.n
     cells = n ** 3
-    g, eng = build_grid(fd, scenes, prec, n, eps, args.x_chunk)
+    g, eng = build_grid(fd, scenes, prec, n, eps, args)
     tiling = eng.tiling()
     g.run(args.warmup, progress_bar=False)
     torch.cuda.synchronize()
@@ -231,9 +234,8 @@ def run_precision(prec, args, dist, fd, scenes, eps, want_halves, want_e2e, samp
         "precision": prec,
         "ms_per_step": ms / args.steps,
         "gcells": cells * args.steps * dist.world / (ms * 1e-3) / 1e9,
-        "launches_per_step": int(tiling[5]),
-        "tiling": {"cells_per_thread_z": int(tiling[0]), "threads_z": int(tiling[1]), "rows_y": int(tiling[2]),
-                   "planes_x": int(tiling[3]), "ctas": int(tiling[4])},
+        "launches_per_step": tiling["launches_per_step"],
+        "tiling": tiling,
         "clocks": clocks,
         "trace": g.detector.E.tensor()[: args.warmup + args.steps].double().cpu(),
         "stats": g.field_stats(),
@@ -272,6 +274,7 @@ def run_precision(prec, args, dist, fd, scenes, eps, want_halves, want_e2e, samp
                       "how": "per step: grid.step() (host waveform -> pinned -> device, fused kernels via the "
                              "C ABI) then the step's detector record copied device -> pinned host"}
     del g, eng
+    gc.collect()  # grids and their components reference each other
     torch.cuda.empty_cache()
     return out
 
@@ -345,7 +348,8 @@ def gb300_arm(args):
         },
         "roofline": {
             "bound": "hbm",
-            "kernel": f"k_update_{kern} ({precs[0]}, fused {kern} half step incl. its small epilogue kernels)",
+            "kernel": f"k_update_{kern}{'_tma' if main['tiling']['variant'] == 2 else ''} ({precs[0]}, fused {kern} "
+                      "half step incl. its small epilogue kernels)",
             "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",

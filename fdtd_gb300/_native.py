@@ -61,6 +61,7 @@ class GridDesc(ctypes.Structure):
     _fields_ = [
         ("abi_version", c_int32), ("precision", c_int32),
         ("nx", c_int32), ("ny", c_int32), ("nz", c_int32), ("x_chunk", c_int32),
+        ("variant", c_int32), ("tile_rows", c_int32), ("stages", c_int32), ("reserved", c_int32),
         ("courant", ctypes.c_double),
         ("E", c_void_p), ("H", c_void_p), ("E_lo", c_void_p), ("H_lo", c_void_p),
         ("inv_eps", c_void_p), ("inv_mu", c_void_p),
@@ -89,6 +90,7 @@ class RunArgs(ctypes.Structure):
 SIGNATURES = {
     "fdtd_plan_create": (c_int32, [ctypes.POINTER(GridDesc), ctypes.POINTER(c_void_p)]),
     "fdtd_plan_destroy": (c_int32, [c_void_p]),
+    "fdtd_plan_status": (c_int32, [c_void_p, ctypes.POINTER(c_int32), c_int32, c_void_p]),
     "fdtd_run": (c_int32, [c_void_p, ctypes.POINTER(RunArgs), c_void_p]),
     "fdtd_curl_E": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p]),
     "fdtd_curl_H": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p]),

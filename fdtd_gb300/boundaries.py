@@ -161,11 +161,25 @@ class PML(Boundary):
         self.c_E = torch.tensor(cE, dtype=dt, device=dev)
         self.b_H = torch.tensor(bH, dtype=dt, device=dev)
         self.c_H = torch.tensor(cH, dtype=dt, device=dev)
-        # compact auxiliaries: [..., 0] drives field[(axis+1)%3], [..., 1] field[(axis+2)%3]
-        self.psi_E = torch.zeros(self.shape + (2,), dtype=dt, device=dev)
-        self.psi_H = torch.zeros(self.shape + (2,), dtype=dt, device=dev)
+        # compact auxiliaries: [..., 0] drives field[(axis+1)%3], [..., 1] field[(axis+2)%3];
+        # a z slab stores an even number of planes (16-byte rows for bulk copies)
+        store = list(self.shape)
+        if axis == 2:
+            store[2] = th + (th % 2)
+        self._psi_E = torch.zeros(tuple(store) + (2,), dtype=dt, device=dev)
+        self._psi_H = torch.zeros(tuple(store) + (2,), dtype=dt, device=dev)
         grid.boundaries.append(self)
         grid._invalidate()
+
+    @property
+    def psi_E(self):
+        """Compact E-side auxiliaries, shape (*slab_shape, 2)."""
+        return self._psi_E[:, :, : self.thickness] if self.axis == 2 else self._psi_E
+
+    @property
+    def psi_H(self):
+        """Compact H-side auxiliaries, shape (*slab_shape, 2)."""
+        return self._psi_H[:, :, : self.thickness] if self.axis == 2 else self._psi_H
 
     # --- reference-shaped views (fdtd/boundaries.py:367-407) ------------------
     @property

@@ -128,6 +128,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.ny = d->ny;
     g.nz = d->nz;
     g.courant = d->courant;
+    g.courant_f = (float)d->courant;
     g.E = d->E;
     g.H = d->H;
     g.Elo = d->E_lo;
@@ -150,6 +151,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             S.high = bd.high ? 1 : 0;
             S.th = bd.thickness;
             S.start = bd.high ? n[bd.axis] - bd.thickness : 0;
+            S.thp = bd.axis == 2 ? bd.thickness + (bd.thickness & 1) : bd.thickness;
             S.psiE = bd.psi_E;
             S.psiH = bd.psi_H;
             S.bE = bd.b_E;
@@ -185,23 +187,110 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     }
 
     // tiling
+    int dev = 0, n_sm = 152, optin = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return cuda_fail(ce);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const int vmax = d->precision == FDTD_FLOAT64 ? PF64::V : PF32::V;
     bool vec = (d->nz % vmax) == 0 && aligned16(d->E) && aligned16(d->H) && aligned16(d->inv_eps) &&
                aligned16(d->inv_mu) && (!comp || (aligned16(d->E_lo) && aligned16(d->H_lo)));
+    if (d->variant < 0 || d->variant > 2) return FDTD_ERR_ARGUMENT;
+    if (d->variant == 2 && !vec) return FDTD_ERR_UNSUPPORTED;
+    // automatic choice: the TMA-staged kernels reach the HBM roofline on grids
+    // without PML; with PML slabs the warps holding slab cells do more work per
+    // plane and the staged kernels' per-plane CTA barrier makes the whole tile
+    // wait for them, so the register-streaming kernels are faster there
+    const bool tma = d->variant == 2 ||
+                     (d->variant == 0 && vec && g.nslab == 0 && (long)d->nz * 3 * (long)esize >= 768);
     Tiling t{};
-    t.V = vec ? vmax : 1;
+    int ctas_per_sm = 2;
+    bool use_tma = tma;
+    if (use_tma) {
+        t.V = vmax;
+        t.TZ = 32;
+        if (d->tile_rows != 0 && d->tile_rows != 4 && d->tile_rows != 8) return FDTD_ERR_ARGUMENT;
+        t.TY = d->tile_rows ? d->tile_rows : 8;
+        // stage layout: field tiles, then one PML auxiliary slot per group of
+        // slabs of one axis that never meet in the same tile (rows copied per stage)
+        const int Zc = 32 * t.V;
+        const size_t field = tma_stage_bytes(d->precision, t.TY);
+        struct Slot {
+            int axis;
+            size_t bytes;
+            std::vector<std::pair<int, int>> ranges;
+            size_t off;
+        };
+        std::vector<Slot> slots;
+        int slot_of[kMaxSlabs] = {0};
+        for (int s = 0; s < g.nslab; ++s) {
+            const SlabK &S = g.slab[s];
+            const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? t.TY : Zc);
+            const std::pair<int, int> rg(S.start / unit, (S.start + S.th - 1) / unit);
+            const int pitch = S.axis == 2 ? 2 * S.thp : 2 * Zc;
+            const size_t bytes = (size_t)t.TY * pitch * esize;
+            g.psi_pitch[s] = pitch;
+            int found = -1;
+            for (int q = 0; q < (int)slots.size() && found < 0; ++q) {
+                if (slots[q].axis != S.axis) continue;
+                bool disjoint = true;
+                for (auto &o : slots[q].ranges)
+                    if (!(rg.second < o.first || o.second < rg.first)) disjoint = false;
+                if (disjoint) found = q;
+            }
+            if (found < 0) {
+                slots.push_back(Slot{S.axis, 0, {}, 0});
+                found = (int)slots.size() - 1;
+            }
+            slots[found].ranges.push_back(rg);
+            slots[found].bytes = std::max(slots[found].bytes, bytes);
+            slot_of[s] = found;
+        }
+        size_t stage = field;
+        for (auto &sl : slots) {
+            sl.off = stage;
+            stage += (sl.bytes + 127) & ~(size_t)127;
+        }
+        for (int s = 0; s < g.nslab; ++s) g.psi_off[s] = (int)slots[slot_of[s]].off;
+        g.stage_bytes = (int)stage;
+        int coef = 0;
+        for (int s = 0; s < g.nslab; ++s) {
+            g.coef_off[s] = coef;
+            coef += 2 * g.slab[s].th;
+        }
+        g.coef_values = (size_t)coef * esize <= 16384 ? coef : 0;
+        const size_t extra = (size_t)g.coef_values * esize + 128;
+        int S = d->stages;
+        if (S == 0) S = (int)std::max<long>(0, std::min<long>(6, ((long)optin - (long)extra) / (long)(stage + 8)));
+        const size_t smem = (size_t)S * stage + (size_t)S * 8 + extra;
+        if (S < 2 || smem > (size_t)optin) {
+            if (d->variant == 2) return FDTD_ERR_UNSUPPORTED;
+            use_tma = false;  // automatic choice: too little shared memory, use the register kernels
+        } else {
+            g.stages = S;
+            ctas_per_sm = std::max(1, (int)((228L * 1024) / (long)(smem + 1024)));
+            p.variant = 2;
+        }
+    }
+    if (!use_tma) {
+        t.V = vec ? vmax : 1;
+        const int zthreads0 = (d->nz + t.V - 1) / t.V;
+        t.TZ = std::min(32, next_pow2(zthreads0));
+        t.TY = kThreads / t.TZ;
+        g.stages = 0;
+        p.variant = 1;
+    }
     const int zthreads = (d->nz + t.V - 1) / t.V;
-    t.TZ = std::min(32, next_pow2(zthreads));
-    t.TY = kThreads / t.TZ;
     t.gz = (zthreads + t.TZ - 1) / t.TZ;
     t.gy = (d->ny + t.TY - 1) / t.TY;
     if (t.gy > 65535) return FDTD_ERR_UNSUPPORTED;
     if (d->x_chunk > 0) {
         t.XC = d->x_chunk;
     } else {
-        // enough CTAs for about four waves of 152 SMs x 2 resident CTAs
+        // split x only when the (z, y) columns do not give two waves of CTAs
         const long cols = (long)t.gz * t.gy;
-        long chunks = (4L * 152 * 2 + cols - 1) / cols;
+        const long target = 2L * n_sm * ctas_per_sm;
+        long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
         chunks = std::max(1L, std::min(chunks, (long)d->nx));
         t.XC = (int)((d->nx + chunks - 1) / chunks);
     }
@@ -334,7 +423,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     const size_t b_lists = align(sizeof(int) * (obj_off.size() + obj_idx.size() + se_off.size() + se_idx.size() +
                                                 sh_off.size() + sh_idx.size() + 6));
     const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
-    std::vector<char> host(b_items + b_lists + b_runs, 0);
+    const size_t b_status = 256;
+    std::vector<char> host(b_items + b_lists + b_runs + b_status, 0);
     if (nitems) memcpy(host.data(), items.data(), sizeof(ItemK) * nitems);
     int *lists = (int *)(host.data() + b_items);
     size_t pos = 0;
@@ -351,7 +441,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     put(sh_off, at_sh_off);
     put(sh_idx, at_sh_idx);
     if (!runs.empty()) memcpy(host.data() + b_items + b_lists, runs.data(), sizeof(int2) * runs.size());
-    cudaError_t ce = cudaMalloc(&p.dev_mem, host.size());
+    ce = cudaMalloc(&p.dev_mem, host.size());
     if (ce != cudaSuccess) return cuda_fail(ce);
     ce = cudaMemcpy(p.dev_mem, host.data(), host.size(), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) {
@@ -369,6 +459,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.srcH_off = dl + at_sh_off;
     g.srcH_idx = dl + at_sh_idx;
     p.runs = (const int2 *)(base + b_items + b_lists);
+    g.status = (int *)(base + b_items + b_lists + b_runs);
+    if (p.variant == 2) {
+        const int rc = d->precision == FDTD_FLOAT32    ? prepare_tma_f32(p)
+                       : d->precision == FDTD_FLOAT32C ? prepare_tma_f32c(p)
+                                                       : prepare_tma_f64(p);
+        if (rc != FDTD_OK) return rc;
+    }
 
     p.stats_ctas = 152 * 4;
     p.launches_per_step = 2 + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
@@ -406,6 +503,18 @@ int fdtd_plan_destroy(fdtd_plan *plan) {
     }
     delete plan;
     return rc;
+}
+
+int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t stream) {
+    if (!plan || !out) return FDTD_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    int v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, plan->p.k.status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && reset) e = cudaMemsetAsync(plan->p.k.status, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e);
+    *out = v;
+    return FDTD_OK;
 }
 
 int fdtd_run(fdtd_plan *plan, const fdtd_run_args *args, fdtd_stream_t stream) {
@@ -475,15 +584,17 @@ int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_s
     return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
 }
 
-int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out6) {
-    if (!plan || !out6) return FDTD_ERR_ARGUMENT;
+int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8) {
+    if (!plan || !out8) return FDTD_ERR_ARGUMENT;
     const Plan &p = plan->p;
-    out6[0] = p.V;
-    out6[1] = p.k.TZ;
-    out6[2] = p.k.TY;
-    out6[3] = p.k.XC;
-    out6[4] = (int64_t)p.grid.x * p.grid.y * p.grid.z;
-    out6[5] = p.launches_per_step;
+    out8[0] = p.V;
+    out8[1] = p.k.TZ;
+    out8[2] = p.k.TY;
+    out8[3] = p.k.XC;
+    out8[4] = (int64_t)p.grid.x * p.grid.y * p.grid.z;
+    out8[5] = p.launches_per_step;
+    out8[6] = p.variant;
+    out8[7] = p.k.stages;
     return FDTD_OK;
 }
 

@@ -1,0 +1,325 @@
+// Per-cell body of the fused half steps, shared by the register-streaming and
+// the TMA-staged kernels.  The caller supplies the six one-sided differences of
+// the neighbour field (zero where the reference drops the out-of-grid
+// difference), the inverse material of the cell and the running field value;
+// the body then applies, in the reference's order (fdtd/grid.py:275-325):
+//   curl and bulk update, objects (E only), PML auxiliaries and corrections,
+//   sources.
+#pragma once
+
+#include "fdtd_common.cuh"
+
+namespace fdtd {
+
+// Where a cell's PML auxiliaries and coefficient tables are read from: the
+// shared-memory stage of the staged kernels, or global memory (stage = null).
+// Updated auxiliaries are always written to global memory.
+template <class T>
+struct PsiSrc {
+    const unsigned char *stage;  // stage base, psi slots at g.psi_off[s]
+    int row;                     // this thread's row in the tile
+    int k0c;                     // first cell of the tile along z
+    const T *ctab;               // b/c tables at g.coef_off[s] (null: global)
+};
+
+// Bit s set: PML slab s can contain cells of this thread.  The y and z parts
+// do not change along x (computed once per thread), the x part per plane.
+__device__ __forceinline__ unsigned slab_mask_yz(const GridK &g, int j, int k0, int V) {
+    unsigned m = 0;
+    for (int s = 0; s < g.nslab; ++s) {
+        const SlabK &S = g.slab[s];
+        if (S.axis == 1) {
+            if ((unsigned)(j - S.start) < (unsigned)S.th) m |= 1u << s;
+        } else if (S.axis == 2) {
+            if (k0 < S.start + S.th && k0 + V > S.start) m |= 1u << s;
+        }
+    }
+    return m;
+}
+
+__device__ __forceinline__ unsigned slab_mask_x(const GridK &g, int i) {
+    unsigned m = 0;
+    for (int s = 0; s < g.nslab; ++s) {
+        const SlabK &S = g.slab[s];
+        if (S.axis == 0 && (unsigned)(i - S.start) < (unsigned)S.th) m |= 1u << s;
+    }
+    return m;
+}
+
+// Objects of one cell (fdtd/objects.py:118-277), in registration order.
+template <class P>
+__device__ __forceinline__ void apply_objects(const GridK &g, int i, int j, int k, typename P::T c, typename P::T cu0,
+                                              typename P::T cu1, typename P::T cu2, typename P::T &ex,
+                                              typename P::T &ey, typename P::T &ez, typename P::T &lx,
+                                              typename P::T &ly, typename P::T &lz, int ob0, int ob1) {
+    using T = typename P::T;
+    for (int it = ob0; it < ob1; ++it) {
+        const ItemK &o = g.items[g.obj_idx[it]];
+        if (!in_box(o, i, j, k)) continue;
+        const size_t li = box_index(o, i, j, k);
+        if (o.kind == FDTD_ITEM_OBJECT) {
+            const T *cf = (const T *)o.coef[0] + 3 * li;
+            P::add_prod(ex, lx, cf[0], cu0);
+            P::add_prod(ey, ly, cf[1], cu1);
+            P::add_prod(ez, lz, cf[2], cu2);
+        } else if (o.kind == FDTD_ITEM_ABSORBING) {
+            const T *r = (const T *)o.coef[0] + 3 * li;
+            const T *ci = (const T *)o.coef[1] + 3 * li;
+            P::scale(ex, lx, r[0]);
+            P::scale(ey, ly, r[1]);
+            P::scale(ez, lz, r[2]);
+            if constexpr (sizeof(T) == 4) {
+                P::add_prod(ex, lx, ci[0], cu0);
+                P::add_prod(ey, ly, ci[1], cu1);
+                P::add_prod(ez, lz, ci[2], cu2);
+            } else {
+                const T *opf = (const T *)o.coef[2] + 3 * li;
+                P::add_quot(ex, lx, ci[0], cu0, opf[0]);
+                P::add_quot(ey, ly, ci[1], cu1, opf[1]);
+                P::add_quot(ez, lz, ci[2], cu2, opf[2]);
+            }
+        } else {
+            const T *M = (const T *)o.coef[0] + 9 * li;
+            P::add_prod(ex, lx, c, P::dot3(M[0], M[1], M[2], cu0, cu1, cu2));
+            P::add_prod(ey, ly, c, P::dot3(M[3], M[4], M[5], cu0, cu1, cu2));
+            P::add_prod(ez, lz, c, P::dot3(M[6], M[7], M[8], cu0, cu1, cu2));
+        }
+    }
+}
+
+// Sources of one cell (fdtd/sources.py:93-109, 278-297, 476-486), in order.
+template <class P>
+__device__ __forceinline__ void apply_sources(const GridK &g, const int *idx, const double *__restrict__ wave, int i,
+                                              int j, int k, typename P::T &fx, typename P::T &fy, typename P::T &fz,
+                                              typename P::T &lx, typename P::T &ly, typename P::T &lz, int sb0,
+                                              int sb1) {
+    using T = typename P::T;
+    for (int it = sb0; it < sb1; ++it) {
+        const ItemK &s = g.items[idx[it]];
+        if (!in_box(s, i, j, k)) continue;
+        const T w = (T)s.weight, wv = (T)wave[s.column];
+        if (s.kind == FDTD_ITEM_SOFT) {
+            if (s.comp == 0) P::add_prod(fx, lx, w, wv);
+            else if (s.comp == 1) P::add_prod(fy, ly, w, wv);
+            else P::add_prod(fz, lz, w, wv);
+        } else {
+            const T val = P::mul(w, wv);
+            if (s.comp == 0) P::set(fx, lx, val);
+            else if (s.comp == 1) P::set(fy, ly, val);
+            else P::set(fz, lz, val);
+        }
+    }
+}
+
+// E += (c m) phi for the E half, H -= (c m) phi for the H half.
+template <class P, bool IS_E>
+__device__ __forceinline__ void pml_correct(typename P::T &f, typename P::T &fl, typename P::T cm, typename P::T phi) {
+    if (IS_E) P::add_prod(f, fl, cm, phi);
+    else P::sub_prod(f, fl, cm, phi);
+}
+
+// PML auxiliaries and corrections of a thread's V cells, slab by slab in
+// boundary order (the per-cell order of fdtd/grid.py:279-291 is kept: every
+// slab touching a cell acts on it in ascending slab order).  d[q][v] are the
+// six one-sided differences of the neighbour field F of cell v, in the order
+// (dx F_y, dx F_z, dy F_x, dy F_z, dz F_x, dz F_y); a slab normal to axis a
+// drives its pair with (dF_(a+2)%3, dF_(a+1)%3) along a.  IS_E selects the E
+// rule (increment at slab-local index >= 1, E += c m phi) or the H rule
+// (index <= th-2, H -= c m phi).
+template <class P, int V, bool IS_E>
+__device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, typename P::T c,
+                                          const typename P::T (&d)[6][V], const typename P::T (&m)[3 * V],
+                                          typename P::T (&f)[3 * V], typename P::T (&fl)[3 * V],
+                                          const PsiSrc<typename P::T> &src, unsigned slabs) {
+    using T = typename P::T;
+    for (unsigned sm = slabs; sm; sm &= sm - 1) {
+        const int s = __ffs(sm) - 1;
+        const SlabK &S = g.slab[s];
+        const int a = S.axis, th = S.th;
+        T *psi = (T *)(IS_E ? S.psiE : S.psiH);
+        const T *bt = (const T *)(IS_E ? S.bE : S.bH);
+        const T *ct = (const T *)(IS_E ? S.cE : S.cH);
+        // slab-local index of cell k0 and the rows of its auxiliaries
+        const int l0 = (a == 0 ? i : (a == 1 ? j : k0)) - S.start;
+        long gofs;
+        if (a == 0) gofs = ((long)l0 * g.ny + j) * g.nz + k0;
+        else if (a == 1) gofs = ((long)i * th + l0) * g.nz + k0;
+        else gofs = ((long)i * g.ny + j) * S.thp + l0;
+        T *gp = psi + 2 * gofs;
+        const T *sp = nullptr;
+        if (src.stage)
+            sp = reinterpret_cast<const T *>(src.stage + g.psi_off[s]) + src.row * g.psi_pitch[s] +
+                 (a == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
+        T bu = T(0), cu = T(0);  // coefficients when l is the same for the V cells
+        if (a != 2) {
+            bu = src.ctab ? src.ctab[g.coef_off[s] + l0] : bt[l0];
+            cu = src.ctab ? src.ctab[g.coef_off[s] + th + l0] : ct[l0];
+        }
+        const bool corr = s < g.nslab_fused;
+        // all loads first (a store to the auxiliaries would otherwise order every
+        // later load behind it), then the updates, then the stores
+        T p0[V], p1[V];
+        if (V > 1 && a != 2) {
+            // x/y slab: the V cells are one contiguous, 16-byte aligned run of pairs
+            alignas(16) T pr[2 * V];
+            if (sp) ld_vec(pr, sp);
+            else ld_vec(pr, (const T *)gp);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                p0[v] = pr[2 * v];
+                p1[v] = pr[2 * v + 1];
+            }
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int l = a == 2 ? l0 + v : l0;
+                p0[v] = T(0);
+                p1[v] = T(0);
+                if ((unsigned)l >= (unsigned)th) continue;
+                if (sp) {
+                    p0[v] = sp[2 * v];
+                    p1[v] = sp[2 * v + 1];
+                } else {
+                    p0[v] = gp[2 * v];
+                    p1[v] = gp[2 * v + 1];
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int l = a == 2 ? l0 + v : l0;
+            if ((unsigned)l >= (unsigned)th) continue;
+            T b = bu, cc = cu;
+            if (a == 2) {
+                b = src.ctab ? src.ctab[g.coef_off[s] + l] : bt[l];
+                cc = src.ctab ? src.ctab[g.coef_off[s] + th + l] : ct[l];
+            }
+            if (IS_E ? (l >= 1) : (l <= th - 2)) {
+                const T d0 = a == 0 ? d[1][v] : (a == 1 ? d[2][v] : d[5][v]);
+                const T d1 = a == 0 ? d[0][v] : (a == 1 ? d[3][v] : d[4][v]);
+                p0[v] = P::psi(p0[v], b, d0, cc);
+                p1[v] = P::psi(p1[v], b, d1, cc);
+            } else {
+                p0[v] = P::mul(p0[v], b);
+                p1[v] = P::mul(p1[v], b);
+            }
+            if (corr) {
+                // phi[(a+1)%3] = -p0, phi[(a+2)%3] = +p1 (fdtd/boundaries.py:457-459, 485-487);
+                // explicit branches keep the field values in registers
+                if (a == 0) {
+                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::mul(c, m[3 * v + 1]), -p0[v]);
+                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::mul(c, m[3 * v + 2]), p1[v]);
+                } else if (a == 1) {
+                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::mul(c, m[3 * v + 2]), -p0[v]);
+                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::mul(c, m[3 * v]), p1[v]);
+                } else {
+                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::mul(c, m[3 * v]), -p0[v]);
+                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::mul(c, m[3 * v + 1]), p1[v]);
+                }
+            }
+        }
+        if (V > 1 && a != 2) {
+            alignas(16) T pr[2 * V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                pr[2 * v] = p0[v];
+                pr[2 * v + 1] = p1[v];
+            }
+            st_vec(gp, pr);
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int l = a == 2 ? l0 + v : l0;
+                if ((unsigned)l >= (unsigned)th) continue;
+                gp[2 * v] = p0[v];
+                gp[2 * v + 1] = p1[v];
+            }
+        }
+    }
+}
+
+// E half step of a thread's V cells at (i, j, k0..k0+V-1).  hc: H of the cells,
+// hp: H at plane i-1, hj: H at row j-1, (kx, ky): Hx, Hy at k0-1.
+template <class P, int V>
+__device__ __forceinline__ void thread_E(const GridK &g, const double *__restrict__ wave, int i, int j, int k0,
+                                         typename P::T c, const typename P::T (&hc)[3 * V],
+                                         const typename P::T (&hp)[3 * V], const typename P::T (&hj)[3 * V],
+                                         typename P::T kx, typename P::T ky, const typename P::T (&m)[3 * V],
+                                         typename P::T (&e)[3 * V], typename P::T (&el)[3 * V], int ob0, int ob1,
+                                         int sb0, int sb1, const PsiSrc<typename P::T> &src, unsigned slabs) {
+    using T = typename P::T;
+    T d[6][V];  // dxHy, dxHz, dyHx, dyHz, dzHx, dzHy (backward, zero on the first plane)
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int k = k0 + v;
+        const T hx = hc[3 * v], hy = hc[3 * v + 1], hz = hc[3 * v + 2];
+        const T pkx = (v > 0) ? hc[3 * (v - 1)] : kx;
+        const T pky = (v > 0) ? hc[3 * (v - 1) + 1] : ky;
+        d[0][v] = (i > 0) ? hy - hp[3 * v + 1] : T(0);
+        d[1][v] = (i > 0) ? hz - hp[3 * v + 2] : T(0);
+        d[2][v] = (j > 0) ? hx - hj[3 * v] : T(0);
+        d[3][v] = (j > 0) ? hz - hj[3 * v + 2] : T(0);
+        d[4][v] = (k > 0) ? hx - pkx : T(0);
+        d[5][v] = (k > 0) ? hy - pky : T(0);
+        const T cu0 = d[3][v] - d[5][v];
+        const T cu1 = d[4][v] - d[1][v];
+        const T cu2 = d[0][v] - d[2][v];
+        P::add_prod(e[3 * v], el[3 * v], P::mul(c, m[3 * v]), cu0);
+        P::add_prod(e[3 * v + 1], el[3 * v + 1], P::mul(c, m[3 * v + 1]), cu1);
+        P::add_prod(e[3 * v + 2], el[3 * v + 2], P::mul(c, m[3 * v + 2]), cu2);
+        if (ob0 < ob1)
+            apply_objects<P>(g, i, j, k, c, cu0, cu1, cu2, e[3 * v], e[3 * v + 1], e[3 * v + 2], el[3 * v],
+                             el[3 * v + 1], el[3 * v + 2], ob0, ob1);
+    }
+    if (slabs) apply_pml<P, V, true>(g, i, j, k0, c, d, m, e, el, src, slabs);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        if (sb0 < sb1)
+            apply_sources<P>(g, g.srcE_idx, wave, i, j, k0 + v, e[3 * v], e[3 * v + 1], e[3 * v + 2], el[3 * v],
+                             el[3 * v + 1], el[3 * v + 2], sb0, sb1);
+        P::finish(e[3 * v], el[3 * v]);
+        P::finish(e[3 * v + 1], el[3 * v + 1]);
+        P::finish(e[3 * v + 2], el[3 * v + 2]);
+    }
+}
+
+// H half step of a thread's V cells.  ec: E of the cells, en: E at plane i+1,
+// ej: E at row j+1, (kx, ky): Ex, Ey at k0+V.
+template <class P, int V>
+__device__ __forceinline__ void thread_H(const GridK &g, const double *__restrict__ wave, int i, int j, int k0,
+                                         typename P::T c, const typename P::T (&ec)[3 * V],
+                                         const typename P::T (&en)[3 * V], const typename P::T (&ej)[3 * V],
+                                         typename P::T kx, typename P::T ky, const typename P::T (&m)[3 * V],
+                                         typename P::T (&h)[3 * V], typename P::T (&hl)[3 * V], int sb0, int sb1,
+                                         const PsiSrc<typename P::T> &src, unsigned slabs) {
+    using T = typename P::T;
+    T d[6][V];  // dxEy, dxEz, dyEx, dyEz, dzEx, dzEy (forward, zero on the last plane)
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int k = k0 + v;
+        const T ex_ = ec[3 * v], ey_ = ec[3 * v + 1], ez_ = ec[3 * v + 2];
+        const T nkx = (v < V - 1) ? ec[3 * (v + 1)] : kx;
+        const T nky = (v < V - 1) ? ec[3 * (v + 1) + 1] : ky;
+        d[0][v] = (i < g.nx - 1) ? en[3 * v + 1] - ey_ : T(0);
+        d[1][v] = (i < g.nx - 1) ? en[3 * v + 2] - ez_ : T(0);
+        d[2][v] = (j < g.ny - 1) ? ej[3 * v] - ex_ : T(0);
+        d[3][v] = (j < g.ny - 1) ? ej[3 * v + 2] - ez_ : T(0);
+        d[4][v] = (k < g.nz - 1) ? nkx - ex_ : T(0);
+        d[5][v] = (k < g.nz - 1) ? nky - ey_ : T(0);
+        P::sub_prod(h[3 * v], hl[3 * v], P::mul(c, m[3 * v]), d[3][v] - d[5][v]);
+        P::sub_prod(h[3 * v + 1], hl[3 * v + 1], P::mul(c, m[3 * v + 1]), d[4][v] - d[1][v]);
+        P::sub_prod(h[3 * v + 2], hl[3 * v + 2], P::mul(c, m[3 * v + 2]), d[0][v] - d[2][v]);
+    }
+    if (slabs) apply_pml<P, V, false>(g, i, j, k0, c, d, m, h, hl, src, slabs);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        if (sb0 < sb1)
+            apply_sources<P>(g, g.srcH_idx, wave, i, j, k0 + v, h[3 * v], h[3 * v + 1], h[3 * v + 2], hl[3 * v],
+                             hl[3 * v + 1], hl[3 * v + 2], sb0, sb1);
+        P::finish(h[3 * v], hl[3 * v]);
+        P::finish(h[3 * v + 1], hl[3 * v + 1]);
+        P::finish(h[3 * v + 2], hl[3 * v + 2]);
+    }
+}
+
+}  // namespace fdtd

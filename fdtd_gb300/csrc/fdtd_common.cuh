@@ -21,6 +21,7 @@ constexpr int kThreads = 256;
 // slab-local plane 0 along `axis`.
 struct SlabK {
     int axis, high, th, start;
+    int thp;  // stored slab-local extent: th, padded to even for z slabs
     void *psiE, *psiH;
     const void *bE, *cE, *bH, *cH;
 };
@@ -39,6 +40,7 @@ struct ItemK {
 struct GridK {
     int nx, ny, nz;
     double courant;
+    float courant_f;  // courant rounded once on the host (float plans)
     void *E, *H, *Elo, *Hlo;
     const void *ie, *imu;
     int nslab;        // PML slabs in boundary order
@@ -50,7 +52,26 @@ struct GridK {
     const int *srcH_off, *srcH_idx;
     int fuse_src_E, fuse_src_H;      // sources applied inside the fused pass
     int TZ, TY, XC;                  // threads along z, rows along y, planes along x per CTA
+    int stages;                      // shared-memory ring depth of the staged (TMA) kernels
+    int *status;                     // device error word (bit 0: a pipeline wait timed out)
+    // staged kernels: bytes of one stage, TMA bytes of the field tiles, and per
+    // slab the byte offset (in a stage) and row pitch (values) of its psi slot
+    int stage_bytes, field_tx;
+    int psi_off[kMaxSlabs], psi_pitch[kMaxSlabs];
+    int coef_off[kMaxSlabs];  // per slab: offset (values) of its b/c tables in shared memory
+    int coef_values;          // values of all staged b/c tables (0: tables are read from global)
 };
+
+template <class T>
+__device__ __forceinline__ T courant_of(const GridK &g);
+template <>
+__device__ __forceinline__ float courant_of<float>(const GridK &g) {
+    return g.courant_f;
+}
+template <>
+__device__ __forceinline__ double courant_of<double>(const GridK &g) {
+    return g.courant;
+}
 
 // ---------------------------------------------------------------------------
 // Precision policies.  The float64 policy reproduces the reference's numpy

@@ -4,4 +4,6 @@
 namespace fdtd {
 int run_f32(Plan &p, const fdtd_run_args *a, cudaStream_t st) { return run_impl<PF32>(p, a, st); }
 int run_f32c(Plan &p, const fdtd_run_args *a, cudaStream_t st) { return run_impl<PF32C>(p, a, st); }
+int prepare_tma_f32(Plan &p) { return prepare_tma_impl<PF32>(p); }
+int prepare_tma_f32c(Plan &p) { return prepare_tma_impl<PF32C>(p); }
 }  // namespace fdtd

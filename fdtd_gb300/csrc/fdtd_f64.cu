@@ -3,4 +3,16 @@
 
 namespace fdtd {
 int run_f64(Plan &p, const fdtd_run_args *a, cudaStream_t st) { return run_impl<PF64>(p, a, st); }
+int prepare_tma_f64(Plan &p) { return prepare_tma_impl<PF64>(p); }
+
+size_t tma_stage_bytes(int precision, int tile_rows) {
+    switch (precision) {
+        case FDTD_FLOAT32:
+            return stage_bytes_of<PF32>(tile_rows);
+        case FDTD_FLOAT32C:
+            return stage_bytes_of<PF32C>(tile_rows);
+        default:
+            return stage_bytes_of<PF64>(tile_rows);
+    }
+}
 }  // namespace fdtd

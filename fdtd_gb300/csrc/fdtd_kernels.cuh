@@ -12,12 +12,15 @@
 // thread streams along x holding the neighbour plane in registers.
 #pragma once
 
-#include "fdtd_common.cuh"
+#include "fdtd_cell.cuh"
 
 namespace fdtd {
 
 #define FULL_MASK 0xffffffffu
 
+// Register-streaming kernels: neighbour values come from global memory
+// (L1/L2) and from the lane to the left/right; used for shapes the staged
+// kernels do not take (nz not a multiple of the vector width, unaligned data).
 template <class P, int V>
 __global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const double *__restrict__ wave) {
     using T = typename P::T;
@@ -30,7 +33,7 @@ __global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const doub
     const int xb = min(nx, xa + g.XC);
     const bool act = (j < ny) && (k0 < nz);
     const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    const T c = (T)g.courant;
+    const T c = courant_of<T>(g);
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
     T *Elo = (T *)g.Elo;
@@ -42,6 +45,8 @@ __global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const doub
         sb1 = g.srcE_off[cta + 1];
     }
 
+    const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
     alignas(16) T hp[N];  // H at plane i-1
 #pragma unroll
     for (int q = 0; q < N; ++q) hp[q] = T(0);
@@ -73,124 +78,8 @@ __global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const doub
             ky = H[3 * (cell0 - 1) + 1];
         }
         if (act) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const int k = k0 + v;
-                const T hx = hc[3 * v], hy = hc[3 * v + 1], hz = hc[3 * v + 2];
-                const T pkx = (v > 0) ? hc[3 * (v - 1)] : kx;
-                const T pky = (v > 0) ? hc[3 * (v - 1) + 1] : ky;
-                // backward differences; zero on the first plane of their axis
-                const T dxHy = (i > 0) ? hy - hp[3 * v + 1] : T(0);
-                const T dxHz = (i > 0) ? hz - hp[3 * v + 2] : T(0);
-                const T dyHx = (j > 0) ? hx - hj[3 * v] : T(0);
-                const T dyHz = (j > 0) ? hz - hj[3 * v + 2] : T(0);
-                const T dzHx = (k > 0) ? hx - pkx : T(0);
-                const T dzHy = (k > 0) ? hy - pky : T(0);
-                const T cu0 = dyHz - dzHy;
-                const T cu1 = dzHx - dxHz;
-                const T cu2 = dxHy - dyHx;
-                T ex = e[3 * v], ey = e[3 * v + 1], ez = e[3 * v + 2];
-                T lx = el[3 * v], ly = el[3 * v + 1], lz = el[3 * v + 2];
-                const T m0 = m[3 * v], m1 = m[3 * v + 1], m2 = m[3 * v + 2];
-                P::add_prod(ex, lx, P::mul(c, m0), cu0);
-                P::add_prod(ey, ly, P::mul(c, m1), cu1);
-                P::add_prod(ez, lz, P::mul(c, m2), cu2);
-
-                for (int it = ob0; it < ob1; ++it) {
-                    const ItemK &o = g.items[g.obj_idx[it]];
-                    if (!in_box(o, i, j, k)) continue;
-                    const size_t li = box_index(o, i, j, k);
-                    if (o.kind == FDTD_ITEM_OBJECT) {
-                        const T *cf = (const T *)o.coef[0] + 3 * li;
-                        P::add_prod(ex, lx, cf[0], cu0);
-                        P::add_prod(ey, ly, cf[1], cu1);
-                        P::add_prod(ez, lz, cf[2], cu2);
-                    } else if (o.kind == FDTD_ITEM_ABSORBING) {
-                        const T *r = (const T *)o.coef[0] + 3 * li;
-                        const T *ci = (const T *)o.coef[1] + 3 * li;
-                        P::scale(ex, lx, r[0]);
-                        P::scale(ey, ly, r[1]);
-                        P::scale(ez, lz, r[2]);
-                        if constexpr (P::COMP || sizeof(T) == 4) {
-                            P::add_prod(ex, lx, ci[0], cu0);
-                            P::add_prod(ey, ly, ci[1], cu1);
-                            P::add_prod(ez, lz, ci[2], cu2);
-                        } else {
-                            const T *opf = (const T *)o.coef[2] + 3 * li;
-                            P::add_quot(ex, lx, ci[0], cu0, opf[0]);
-                            P::add_quot(ey, ly, ci[1], cu1, opf[1]);
-                            P::add_quot(ez, lz, ci[2], cu2, opf[2]);
-                        }
-                    } else {
-                        const T *M = (const T *)o.coef[0] + 9 * li;
-                        P::add_prod(ex, lx, c, P::dot3(M[0], M[1], M[2], cu0, cu1, cu2));
-                        P::add_prod(ey, ly, c, P::dot3(M[3], M[4], M[5], cu0, cu1, cu2));
-                        P::add_prod(ez, lz, c, P::dot3(M[6], M[7], M[8], cu0, cu1, cu2));
-                    }
-                }
-
-                for (int s = 0; s < g.nslab; ++s) {
-                    const SlabK &S = g.slab[s];
-                    const int a = S.axis;
-                    const int l = (a == 0 ? i : (a == 1 ? j : k)) - S.start;
-                    if ((unsigned)l >= (unsigned)S.th) continue;
-                    const size_t pidx = a == 0   ? ((size_t)l * ny + j) * nz + k
-                                        : a == 1 ? ((size_t)i * S.th + l) * nz + k
-                                                 : ((size_t)i * ny + j) * S.th + l;
-                    T *pp = (T *)S.psiE + 2 * pidx;
-                    T p0 = pp[0], p1 = pp[1];
-                    const T b = ((const T *)S.bE)[l];
-                    if (l >= 1) {
-                        const T cc = ((const T *)S.cE)[l];
-                        const T d0 = a == 0 ? dxHz : (a == 1 ? dyHx : dzHy);
-                        const T d1 = a == 0 ? dxHy : (a == 1 ? dyHz : dzHx);
-                        p0 = P::psi(p0, b, d0, cc);
-                        p1 = P::psi(p1, b, d1, cc);
-                    } else {
-                        p0 = P::mul(p0, b);
-                        p1 = P::mul(p1, b);
-                    }
-                    pp[0] = p0;
-                    pp[1] = p1;
-                    if (s < g.nslab_fused) {
-                        if (a == 0) {
-                            P::add_prod(ey, ly, P::mul(c, m1), -p0);
-                            P::add_prod(ez, lz, P::mul(c, m2), p1);
-                        } else if (a == 1) {
-                            P::add_prod(ez, lz, P::mul(c, m2), -p0);
-                            P::add_prod(ex, lx, P::mul(c, m0), p1);
-                        } else {
-                            P::add_prod(ex, lx, P::mul(c, m0), -p0);
-                            P::add_prod(ey, ly, P::mul(c, m1), p1);
-                        }
-                    }
-                }
-
-                for (int it = sb0; it < sb1; ++it) {
-                    const ItemK &s = g.items[g.srcE_idx[it]];
-                    if (!in_box(s, i, j, k)) continue;
-                    const T w = (T)s.weight, wv = (T)wave[s.column];
-                    if (s.kind == FDTD_ITEM_SOFT) {
-                        if (s.comp == 0) P::add_prod(ex, lx, w, wv);
-                        else if (s.comp == 1) P::add_prod(ey, ly, w, wv);
-                        else P::add_prod(ez, lz, w, wv);
-                    } else {
-                        const T val = P::mul(w, wv);
-                        if (s.comp == 0) P::set(ex, lx, val);
-                        else if (s.comp == 1) P::set(ey, ly, val);
-                        else P::set(ez, lz, val);
-                    }
-                }
-                P::finish(ex, lx);
-                P::finish(ey, ly);
-                P::finish(ez, lz);
-                e[3 * v] = ex;
-                e[3 * v + 1] = ey;
-                e[3 * v + 2] = ez;
-                el[3 * v] = lx;
-                el[3 * v + 1] = ly;
-                el[3 * v + 2] = lz;
-            }
+            const unsigned slabs = mask_yz | slab_mask_x(g, i);
+            thread_E<P, V>(g, wave, i, j, k0, c, hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage, slabs);
             st_vec(E + 3 * cell0, e);
             if constexpr (P::COMP) st_vec(Elo + 3 * cell0, el);
         }
@@ -211,7 +100,7 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
     const int xb = min(nx, xa + g.XC);
     const bool act = (j < ny) && (k0 < nz);
     const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    const T c = (T)g.courant;
+    const T c = courant_of<T>(g);
     const T *__restrict__ E = (const T *)g.E;
     T *H = (T *)g.H;
     T *Hlo = (T *)g.Hlo;
@@ -222,6 +111,8 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
         sb1 = g.srcH_off[cta + 1];
     }
 
+    const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
     alignas(16) T ec[N];  // E at plane i
 #pragma unroll
     for (int q = 0; q < N; ++q) ec[q] = T(0);
@@ -253,91 +144,8 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
             ky = E[3 * (cell0 + V) + 1];
         }
         if (act) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const int k = k0 + v;
-                const T ex_ = ec[3 * v], ey_ = ec[3 * v + 1], ez_ = ec[3 * v + 2];
-                const T nkx = (v < V - 1) ? ec[3 * (v + 1)] : kx;
-                const T nky = (v < V - 1) ? ec[3 * (v + 1) + 1] : ky;
-                // forward differences; zero on the last plane of their axis
-                const T dxEy = (i < nx - 1) ? en[3 * v + 1] - ey_ : T(0);
-                const T dxEz = (i < nx - 1) ? en[3 * v + 2] - ez_ : T(0);
-                const T dyEx = (j < ny - 1) ? ej[3 * v] - ex_ : T(0);
-                const T dyEz = (j < ny - 1) ? ej[3 * v + 2] - ez_ : T(0);
-                const T dzEx = (k < nz - 1) ? nkx - ex_ : T(0);
-                const T dzEy = (k < nz - 1) ? nky - ey_ : T(0);
-                const T cu0 = dyEz - dzEy;
-                const T cu1 = dzEx - dxEz;
-                const T cu2 = dxEy - dyEx;
-                T hx = h[3 * v], hy = h[3 * v + 1], hz = h[3 * v + 2];
-                T lx = hl[3 * v], ly = hl[3 * v + 1], lz = hl[3 * v + 2];
-                const T m0 = m[3 * v], m1 = m[3 * v + 1], m2 = m[3 * v + 2];
-                P::sub_prod(hx, lx, P::mul(c, m0), cu0);
-                P::sub_prod(hy, ly, P::mul(c, m1), cu1);
-                P::sub_prod(hz, lz, P::mul(c, m2), cu2);
-
-                for (int s = 0; s < g.nslab; ++s) {
-                    const SlabK &S = g.slab[s];
-                    const int a = S.axis;
-                    const int l = (a == 0 ? i : (a == 1 ? j : k)) - S.start;
-                    if ((unsigned)l >= (unsigned)S.th) continue;
-                    const size_t pidx = a == 0   ? ((size_t)l * ny + j) * nz + k
-                                        : a == 1 ? ((size_t)i * S.th + l) * nz + k
-                                                 : ((size_t)i * ny + j) * S.th + l;
-                    T *pp = (T *)S.psiH + 2 * pidx;
-                    T p0 = pp[0], p1 = pp[1];
-                    const T b = ((const T *)S.bH)[l];
-                    if (l <= S.th - 2) {
-                        const T cc = ((const T *)S.cH)[l];
-                        const T d0 = a == 0 ? dxEz : (a == 1 ? dyEx : dzEy);
-                        const T d1 = a == 0 ? dxEy : (a == 1 ? dyEz : dzEx);
-                        p0 = P::psi(p0, b, d0, cc);
-                        p1 = P::psi(p1, b, d1, cc);
-                    } else {
-                        p0 = P::mul(p0, b);
-                        p1 = P::mul(p1, b);
-                    }
-                    pp[0] = p0;
-                    pp[1] = p1;
-                    if (s < g.nslab_fused) {
-                        if (a == 0) {
-                            P::sub_prod(hy, ly, P::mul(c, m1), -p0);
-                            P::sub_prod(hz, lz, P::mul(c, m2), p1);
-                        } else if (a == 1) {
-                            P::sub_prod(hz, lz, P::mul(c, m2), -p0);
-                            P::sub_prod(hx, lx, P::mul(c, m0), p1);
-                        } else {
-                            P::sub_prod(hx, lx, P::mul(c, m0), -p0);
-                            P::sub_prod(hy, ly, P::mul(c, m1), p1);
-                        }
-                    }
-                }
-
-                for (int it = sb0; it < sb1; ++it) {
-                    const ItemK &s = g.items[g.srcH_idx[it]];
-                    if (!in_box(s, i, j, k)) continue;
-                    const T w = (T)s.weight, wv = (T)wave[s.column];
-                    if (s.kind == FDTD_ITEM_SOFT) {
-                        if (s.comp == 0) P::add_prod(hx, lx, w, wv);
-                        else if (s.comp == 1) P::add_prod(hy, ly, w, wv);
-                        else P::add_prod(hz, lz, w, wv);
-                    } else {
-                        const T val = P::mul(w, wv);
-                        if (s.comp == 0) P::set(hx, lx, val);
-                        else if (s.comp == 1) P::set(hy, ly, val);
-                        else P::set(hz, lz, val);
-                    }
-                }
-                P::finish(hx, lx);
-                P::finish(hy, ly);
-                P::finish(hz, lz);
-                h[3 * v] = hx;
-                h[3 * v + 1] = hy;
-                h[3 * v + 2] = hz;
-                hl[3 * v] = lx;
-                hl[3 * v + 1] = ly;
-                hl[3 * v + 2] = lz;
-            }
+            const unsigned slabs = mask_yz | slab_mask_x(g, i);
+            thread_H<P, V>(g, wave, i, j, k0, c, ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
             st_vec(H + 3 * cell0, h);
             if constexpr (P::COMP) st_vec(Hlo + 3 * cell0, hl);
         }
@@ -384,8 +192,9 @@ __global__ void k_slab_correct(const GridK g, int s) {
     const SlabK &S = g.slab[s];
     const int a = S.axis;
     const int n0 = a == 0 ? S.th : g.nx, n1 = a == 1 ? S.th : g.ny, n2 = a == 2 ? S.th : g.nz;
+    const int p2 = a == 2 ? S.thp : g.nz;  // stored extent of the last axis
     const long total = (long)n0 * n1 * n2;
-    const T c = (T)g.courant;
+    const T c = courant_of<T>(g);
     T *F = (T *)(IS_E ? g.E : g.H);
     T *Flo = (T *)(IS_E ? g.Elo : g.Hlo);
     const T *M = (const T *)(IS_E ? g.ie : g.imu);
@@ -394,7 +203,8 @@ __global__ void k_slab_correct(const GridK g, int s) {
         const int i0 = (int)(t / ((long)n1 * n2)), i1 = (int)((t / n2) % n1), i2 = (int)(t % n2);
         const int gi = a == 0 ? i0 + S.start : i0, gj = a == 1 ? i1 + S.start : i1, gk = a == 2 ? i2 + S.start : i2;
         const size_t cell = ((size_t)gi * g.ny + gj) * g.nz + gk;
-        const T p0 = psi[2 * t], p1 = psi[2 * t + 1];
+        const size_t pt = ((size_t)i0 * n1 + i1) * p2 + i2;
+        const T p0 = psi[2 * pt], p1 = psi[2 * pt + 1];
         const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
         T x1 = F[3 * cell + t1], x2 = F[3 * cell + t2];
         T l1 = T(0), l2 = T(0);

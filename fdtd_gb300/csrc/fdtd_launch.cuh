@@ -1,8 +1,11 @@
 // Launch sequence of one fdtd_run call, templated on the precision policy.
 #pragma once
 
+#include <cudaTypedefs.h>
+
 #include "fdtd_kernels.cuh"
 #include "fdtd_plan.hpp"
+#include "fdtd_tma.cuh"
 
 namespace fdtd {
 
@@ -16,9 +19,26 @@ static int check_launch() {
     return FDTD_OK;
 }
 
+template <class P, int TY>
+static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
+    const dim3 block(kTmaTZ, TY, 1);
+    const CUtensorMap *m = p.maps;
+    if (is_E)
+        k_update_E_tma<P, TY><<<p.grid, block, p.smem_bytes, st>>>(
+            p.k, wave, m[MAP_H_NBR], m[MAP_E_OWN], m[MAP_IE], m[P::COMP ? MAP_ELO : MAP_E_OWN]);
+    else
+        k_update_H_tma<P, TY><<<p.grid, block, p.smem_bytes, st>>>(
+            p.k, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
+}
+
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
+    if (p.variant == 2) {
+        if (p.k.TY == 8) launch_tma<P, 8>(p, is_E, wave, st);
+        else launch_tma<P, 4>(p, is_E, wave, st);
+        return;
+    }
     if (p.V == 1) {
         if (is_E) k_update_E<P, 1><<<p.grid, p.block, 0, st>>>(p.k, wave);
         else k_update_H<P, 1><<<p.grid, p.block, 0, st>>>(p.k, wave);
@@ -65,6 +85,76 @@ static void launch_epilogue(Plan &p, bool is_E, const double *wave, cudaStream_t
             }
         }
     }
+}
+
+// --- TMA-staged plan preparation ------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (fn == nullptr) {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+    return fn;
+}
+
+// 2D view of an (nx, ny, nz, 3) field: rows = nx*ny, row = 3*nz values, as
+// 8-byte elements; box = box_w elements by box_rows rows.
+static bool encode_field_map(CUtensorMap *m, const void *base, const GridK &g, int esize, int box_w, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (enc == nullptr || base == nullptr) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)g.nz * 3 * esize / 8, (cuuint64_t)g.nx * g.ny};
+    cuuint64_t strides[1] = {(cuuint64_t)g.nz * 3 * esize};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void *>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+template <class P, int TY>
+static int prepare_tma_rows(Plan &p) {
+    using G = StageGeom<typename P::T, TY, P::COMP>;
+    const GridK &g = p.k;
+    const int es = (int)sizeof(typename P::T);
+    bool ok = encode_field_map(&p.maps[MAP_H_NBR], g.H, g, es, G::boxN, TY + 1) &&
+              encode_field_map(&p.maps[MAP_E_NBR], g.E, g, es, G::boxN, TY + 1) &&
+              encode_field_map(&p.maps[MAP_E_OWN], g.E, g, es, G::boxO, TY) &&
+              encode_field_map(&p.maps[MAP_H_OWN], g.H, g, es, G::boxO, TY) &&
+              encode_field_map(&p.maps[MAP_IE], g.ie, g, es, G::boxO, TY) &&
+              encode_field_map(&p.maps[MAP_MU], g.imu, g, es, G::boxO, TY);
+    if (ok && P::COMP)
+        ok = encode_field_map(&p.maps[MAP_ELO], g.Elo, g, es, G::boxO, TY) &&
+             encode_field_map(&p.maps[MAP_HLO], g.Hlo, g, es, G::boxO, TY);
+    if (!ok) return FDTD_ERR_UNSUPPORTED;
+    p.k.field_tx = (int)G::txBytes;
+    p.smem_bytes = (size_t)g.stages * g.stage_bytes + (size_t)g.stages * 8 +
+                   (size_t)g.coef_values * sizeof(typename P::T) + 128;
+    cudaError_t e = cudaFuncSetAttribute(k_update_E_tma<P, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p.smem_bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_update_H_tma<P, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)p.smem_bytes);
+    if (e != cudaSuccess) {
+        set_last_cuda_error((int)e);
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+template <class P>
+static int prepare_tma_impl(Plan &p) {
+    return p.k.TY == 8 ? prepare_tma_rows<P, 8>(p) : prepare_tma_rows<P, 4>(p);
+}
+
+template <class P>
+static size_t stage_bytes_of(int tile_rows) {
+    return tile_rows == 8 ? (size_t)StageGeom<typename P::T, 8, P::COMP>::stageBytes
+                          : (size_t)StageGeom<typename P::T, 4, P::COMP>::stageBytes;
 }
 
 template <class P>

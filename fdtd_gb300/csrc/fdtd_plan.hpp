@@ -3,6 +3,8 @@
 // pass when a periodic boundary fixes the order of the later stages.
 #pragma once
 
+#include <cuda.h>
+
 #include <vector>
 
 #include "fdtd_common.cuh"
@@ -20,11 +22,17 @@ struct EpiOp {
     int run_count;
 };
 
+// Tensor maps of the TMA-staged kernels (one 2D view per field and box shape).
+enum MapId { MAP_H_NBR = 0, MAP_E_NBR, MAP_E_OWN, MAP_H_OWN, MAP_IE, MAP_MU, MAP_ELO, MAP_HLO, MAP_COUNT };
+
 struct Plan {
     int precision;
     GridK k;
     int V;             // cells per thread along z
     dim3 grid, block;  // fused-pass launch shape
+    int variant;       // 1 register streaming, 2 TMA-staged
+    size_t smem_bytes; // dynamic shared memory of the TMA-staged kernels
+    CUtensorMap maps[MAP_COUNT];
     std::vector<EpiOp> epi_E, epi_H;
     const int2 *runs;  // device, soft-source runs for EPI_SOFT
     int n_probe;
@@ -40,6 +48,13 @@ struct Plan {
 int run_f32(Plan &p, const fdtd_run_args *a, cudaStream_t st);
 int run_f32c(Plan &p, const fdtd_run_args *a, cudaStream_t st);
 int run_f64(Plan &p, const fdtd_run_args *a, cudaStream_t st);
+
+// Stage size in bytes of the TMA-staged kernels for a precision and tile rows.
+size_t tma_stage_bytes(int precision, int tile_rows);
+// Tensor maps and the shared-memory attribute of the TMA-staged kernels.
+int prepare_tma_f32(Plan &p);
+int prepare_tma_f32c(Plan &p);
+int prepare_tma_f64(Plan &p);
 
 void set_last_cuda_error(int e);
 

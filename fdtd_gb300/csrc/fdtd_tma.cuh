@@ -1,0 +1,387 @@
+// TMA-staged fused half steps.
+//
+// A CTA of 32 x TY threads owns a tile of TY rows (y) by 32*V cells (z) and
+// marches along x over a chunk of planes.  Each field is viewed as a 2D
+// tensor of (nx*ny) rows by 3*nz values (8-byte elements for the tensor map)
+// and one TMA load per field and plane fills a shared-memory stage:
+//
+//   E half: H tile of TY+1 rows (row 0 = j0-1) with a 4-value prefix that
+//           holds the cell k0-1, plus the E, inverse-permittivity (and
+//           compensation) tiles of TY rows;
+//   H half: E tile of TY+1 rows (row TY = j0+TY) with a 4-value suffix that
+//           holds the cell k0+32V, plus the H, inverse-permeability (and
+//           compensation) tiles.  Plane i needs E(i) and E(i+1), so two
+//           stages are read at once.
+//
+// A ring of S stages keeps S-1 planes of loads in flight while the threads
+// compute from shared memory; the E half keeps H(i-1) in registers.  The
+// tiles reach past the grid edges where the differences are dropped; the
+// TMA unit fills out-of-range rows and columns with zeros.  Every mbarrier
+// wait is bounded: on expiry the CTA records bit 0 in the plan's status word,
+// drains its outstanding copies (bounded again) and returns.
+#pragma once
+
+#include <cuda.h>
+
+#include "fdtd_cell.cuh"
+
+namespace fdtd {
+
+constexpr int kTmaTZ = 32;
+constexpr unsigned kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Byte layout of the field part of one stage: the neighbour tile (TY+1 rows
+// of 3*Zc+4 values) then the own tiles (TY rows of 3*Zc values each),
+// 128-byte aligned.  The PML auxiliary slots follow at g.psi_off[s].
+template <class T, int TY, bool COMP>
+struct StageGeom {
+    static constexpr int V = sizeof(T) == 4 ? 4 : 2;
+    static constexpr int Zc = kTmaTZ * V;  // cells per tile row
+    static constexpr int pitchN = 3 * Zc + 4;  // values per neighbour row
+    static constexpr int pitchO = 3 * Zc;
+    static constexpr int nbrBytes = (TY + 1) * pitchN * (int)sizeof(T);
+    static constexpr int ownBytes = TY * pitchO * (int)sizeof(T);
+    static constexpr int nOwn = COMP ? 3 : 2;
+    static constexpr int al(int v) { return (v + 127) & ~127; }
+    static constexpr int ownOff = al(nbrBytes);
+    static constexpr int ownStride = al(ownBytes);
+    static constexpr int stageBytes = ownOff + nOwn * ownStride;
+    static constexpr uint32_t txBytes = (uint32_t)(nbrBytes + nOwn * ownBytes);
+    // tensor-map boxes in 8-byte elements
+    static constexpr int boxN = pitchN * (int)sizeof(T) / 8;
+    static constexpr int boxO = pitchO * (int)sizeof(T) / 8;
+};
+
+// Fill one stage for plane p (warp 0, all lanes).  The PML auxiliary rows of
+// every slab crossing the tile at plane p are copied with 1D bulk copies (one
+// row per lane), then lane 0 arms the stage barrier with the total byte count
+// and issues the field tiles.
+template <class T, int TY>
+__device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, uint32_t bar, int p, bool with_psi,
+                                           bool is_E, int k0c, int j0, int Zc, const CUtensorMap *tmN, int xN,
+                                           int yN, const CUtensorMap *tmF, const CUtensorMap *tmM,
+                                           const CUtensorMap *tmL, bool comp, int xO, int ownOff, int ownStride) {
+    const int lane = threadIdx.x;
+    uint32_t bytes[2] = {0u, 0u};
+    const void *srcp[2] = {nullptr, nullptr};
+    uint32_t dst[2] = {0u, 0u};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int q = lane + 32 * h;
+        const int s = q / TY, rr = q % TY;
+        const int j = j0 + rr;
+        if (!with_psi || s >= g.nslab || j >= g.ny) continue;
+        const SlabK &S = g.slab[s];
+        const T *psi = (const T *)(is_E ? S.psiE : S.psiH);
+        const int cells = min(Zc, g.nz - k0c);
+        size_t off;
+        uint32_t nb;
+        if (S.axis == 0) {
+            const int l = p - S.start;
+            if ((unsigned)l >= (unsigned)S.th) continue;
+            off = (((size_t)l * g.ny + j) * g.nz + k0c) * 2;
+            nb = (uint32_t)(2 * cells * sizeof(T));
+        } else if (S.axis == 1) {
+            const int l = j - S.start;
+            if ((unsigned)l >= (unsigned)S.th) continue;
+            off = (((size_t)p * S.th + l) * g.nz + k0c) * 2;
+            nb = (uint32_t)(2 * cells * sizeof(T));
+        } else {
+            if (k0c >= S.start + S.th || k0c + Zc <= S.start) continue;
+            off = ((size_t)p * g.ny + j) * S.thp * 2;
+            nb = (uint32_t)(2 * S.thp * sizeof(T));
+        }
+        bytes[h] = nb;
+        srcp[h] = psi + off;
+        dst[h] = smem_u32(st + g.psi_off[s] + (size_t)rr * g.psi_pitch[s] * sizeof(T));
+    }
+    const uint32_t tot = __reduce_add_sync(0xffffffffu, bytes[0] + bytes[1]);
+    if (lane == 0) mbar_expect_tx(bar, (uint32_t)g.field_tx + tot);
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (bytes[h]) bulk_copy_g2s(dst[h], srcp[h], bytes[h], bar);
+    if (lane == 0) {
+        tma_load_2d(smem_u32(st), tmN, xN, yN, bar);
+        tma_load_2d(smem_u32(st + ownOff), tmF, xO, yN + (is_E ? 1 : 0), bar);
+        tma_load_2d(smem_u32(st + ownOff + ownStride), tmM, xO, yN + (is_E ? 1 : 0), bar);
+        if (comp) tma_load_2d(smem_u32(st + ownOff + 2 * ownStride), tmL, xO, yN + (is_E ? 1 : 0), bar);
+    }
+}
+
+// Copy the PML b/c tables of the half step into shared memory (all threads).
+template <class T>
+__device__ __forceinline__ void stage_coef_tables(const GridK &g, T *tab, bool is_E) {
+    const int nthr = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int s = 0; s < g.nslab; ++s) {
+        const SlabK &S = g.slab[s];
+        const T *b = (const T *)(is_E ? S.bE : S.bH);
+        const T *c = (const T *)(is_E ? S.cE : S.cH);
+        for (int t = tid; t < 2 * S.th; t += nthr) tab[g.coef_off[s] + t] = t < S.th ? b[t] : c[t - S.th];
+    }
+}
+
+template <class P, int TY>
+__global__ void __launch_bounds__(kTmaTZ *TY)
+    k_update_E_tma(const GridK g, const double *__restrict__ wave, const __grid_constant__ CUtensorMap tmN,
+                   const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmM,
+                   const __grid_constant__ CUtensorMap tmL) {
+    using T = typename P::T;
+    using G = StageGeom<T, TY, P::COMP>;
+    constexpr int V = G::V;
+    constexpr int N = 3 * V;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ int abort_flag;
+    // TMA destinations must be 128-byte aligned; the launch adds 128 bytes of slack
+    unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+    const int S = g.stages;
+    const int SB = g.stage_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)S * SB);
+    T *ctab = reinterpret_cast<T *>(smem + (size_t)S * SB + 8 * (size_t)S);
+    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kTmaTZ + tz;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
+    const int k0 = k0c + tz * V, j = j0 + ty;
+    const int xa = blockIdx.z * g.XC, xb = min(nx, xa + g.XC);
+    const int np = xb - xa;
+    const bool act = (j < ny) && (k0 < nz);
+    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const T c = courant_of<T>(g);
+    const T *__restrict__ H = (const T *)g.H;
+    T *E = (T *)g.E;
+    T *Elo = (T *)g.Elo;
+    const int ob0 = g.obj_off[cta], ob1 = g.obj_off[cta + 1];
+    int sb0 = 0, sb1 = 0;
+    if (g.fuse_src_E) {
+        sb0 = g.srcE_off[cta];
+        sb1 = g.srcE_off[cta + 1];
+    }
+    const int xN = (3 * k0c - 4) * (int)sizeof(T) / 8;  // neighbour tile starts 4 values early
+    const int xO = 3 * k0c * (int)sizeof(T) / 8;
+
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < S; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    if (g.coef_values) stage_coef_tables<T>(g, ctab, true);
+    __syncthreads();
+
+    auto issue = [&](int r) {
+        const int p = xa + r;
+        fill_stage<T, TY>(g, smem + (size_t)(r % S) * SB, smem_u32(&bars[r % S]), p, true, true, k0c, j0, G::Zc,
+                          &tmN, xN, p * ny + j0 - 1, &tmF, &tmM, &tmL, P::COMP, xO, G::ownOff, G::ownStride);
+    };
+    int issued = 0;
+    for (; issued < min(S, np); ++issued)
+        if (ty == 0) issue(issued);
+
+    const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
+    alignas(16) T hp[N];  // H at plane i-1 (registers)
+#pragma unroll
+    for (int q = 0; q < N; ++q) hp[q] = T(0);
+    if (act && xa > 0) ld_vec_ro(hp, H + 3 * (((size_t)(xa - 1) * ny + j) * nz + k0));
+
+    int r = 0;
+    for (; r < np; ++r) {
+        const int i = xa + r;
+        const unsigned char *st = smem + (size_t)(r % S) * SB;
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[r % S]), (uint32_t)((r / S) & 1));
+        if (!ok) abort_flag = 1;
+        if (act && ok) {
+            const T *Hn = reinterpret_cast<const T *>(st);
+            const T *Ef = reinterpret_cast<const T *>(st + G::ownOff);
+            const T *Mf = reinterpret_cast<const T *>(st + G::ownOff + G::ownStride);
+            const int on = (ty + 1) * G::pitchN + 4 + 3 * tz * V;  // own row in the neighbour tile
+            const int oo = ty * G::pitchO + 3 * tz * V;
+            alignas(16) T hc[N], hj[N], e[N], el[N], m[N];
+            ld_vec(hc, Hn + on);
+            ld_vec(hj, Hn + on - G::pitchN);
+            ld_vec(e, Ef + oo);
+            ld_vec(m, Mf + oo);
+            if constexpr (P::COMP) {
+                ld_vec(el, reinterpret_cast<const T *>(st + G::ownOff + 2 * G::ownStride) + oo);
+            } else {
+#pragma unroll
+                for (int q = 0; q < N; ++q) el[q] = T(0);
+            }
+            const T kx = Hn[on - 3], ky = Hn[on - 2];  // cell k0-1 (prefix when tz == 0)
+            const PsiSrc<T> src{st, ty, k0c, g.coef_values ? ctab : nullptr};
+            const unsigned slabs = mask_yz | slab_mask_x(g, i);
+            thread_E<P, V>(g, wave, i, j, k0, c, hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, src, slabs);
+            const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
+            st_vec(E + 3 * cell0, e);
+            if constexpr (P::COMP) st_vec(Elo + 3 * cell0, el);
+#pragma unroll
+            for (int q = 0; q < N; ++q) hp[q] = hc[q];
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        if (issued < np) {
+            if (ty == 0) {
+                fence_proxy_async();
+                issue(issued);
+            }
+            ++issued;
+        }
+    }
+    if (abort_flag && tid == 0) {
+        atomicOr(g.status, 1);
+        for (int q = r; q < issued; ++q) mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1));
+    }
+}
+
+template <class P, int TY>
+__global__ void __launch_bounds__(kTmaTZ *TY)
+    k_update_H_tma(const GridK g, const double *__restrict__ wave, const __grid_constant__ CUtensorMap tmN,
+                   const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmM,
+                   const __grid_constant__ CUtensorMap tmL) {
+    using T = typename P::T;
+    using G = StageGeom<T, TY, P::COMP>;
+    constexpr int V = G::V;
+    constexpr int N = 3 * V;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ int abort_flag;
+    unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+    const int S = g.stages;
+    const int SB = g.stage_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)S * SB);
+    T *ctab = reinterpret_cast<T *>(smem + (size_t)S * SB + 8 * (size_t)S);
+    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kTmaTZ + tz;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
+    const int k0 = k0c + tz * V, j = j0 + ty;
+    const int xa = blockIdx.z * g.XC, xb = min(nx, xa + g.XC);
+    const int np = xb - xa;
+    const int nfill = np + 1;  // E of plane xb is needed by the last plane
+    const bool act = (j < ny) && (k0 < nz);
+    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const T c = courant_of<T>(g);
+    T *H = (T *)g.H;
+    T *Hlo = (T *)g.Hlo;
+    int sb0 = 0, sb1 = 0;
+    if (g.fuse_src_H) {
+        sb0 = g.srcH_off[cta];
+        sb1 = g.srcH_off[cta + 1];
+    }
+    const int xO = 3 * k0c * (int)sizeof(T) / 8;
+
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < S; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    if (g.coef_values) stage_coef_tables<T>(g, ctab, false);
+    __syncthreads();
+
+    auto issue = [&](int r) {
+        const int p = xa + r;
+        fill_stage<T, TY>(g, smem + (size_t)(r % S) * SB, smem_u32(&bars[r % S]), p, p < xb, false, k0c, j0,
+                          G::Zc, &tmN, xO, p * ny + j0, &tmF, &tmM, &tmL, P::COMP, xO, G::ownOff, G::ownStride);
+    };
+    int issued = 0;
+    for (; issued < min(S, nfill); ++issued)
+        if (ty == 0) issue(issued);
+
+    const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
+    int r = 0;
+    for (; r < np; ++r) {
+        const int i = xa + r;
+        const unsigned char *st = smem + (size_t)(r % S) * SB;
+        const unsigned char *sn = smem + (size_t)((r + 1) % S) * SB;
+        bool ok = mbar_wait_bounded(smem_u32(&bars[r % S]), (uint32_t)((r / S) & 1));
+        ok = ok && mbar_wait_bounded(smem_u32(&bars[(r + 1) % S]), (uint32_t)(((r + 1) / S) & 1));
+        if (!ok) abort_flag = 1;
+        if (act && ok) {
+            const T *En = reinterpret_cast<const T *>(st);
+            const T *Ex1 = reinterpret_cast<const T *>(sn);
+            const T *Hf = reinterpret_cast<const T *>(st + G::ownOff);
+            const T *Mf = reinterpret_cast<const T *>(st + G::ownOff + G::ownStride);
+            const int on = ty * G::pitchN + 3 * tz * V;
+            const int oo = ty * G::pitchO + 3 * tz * V;
+            alignas(16) T ec[N], en[N], ej[N], h[N], hl[N], m[N];
+            ld_vec(ec, En + on);
+            ld_vec(ej, En + on + G::pitchN);
+            ld_vec(en, Ex1 + on);
+            ld_vec(h, Hf + oo);
+            ld_vec(m, Mf + oo);
+            if constexpr (P::COMP) {
+                ld_vec(hl, reinterpret_cast<const T *>(st + G::ownOff + 2 * G::ownStride) + oo);
+            } else {
+#pragma unroll
+                for (int q = 0; q < N; ++q) hl[q] = T(0);
+            }
+            const T kx = En[on + N], ky = En[on + N + 1];  // cell k0+V (suffix for the last lane)
+            const PsiSrc<T> src{st, ty, k0c, g.coef_values ? ctab : nullptr};
+            const unsigned slabs = mask_yz | slab_mask_x(g, i);
+            thread_H<P, V>(g, wave, i, j, k0, c, ec, en, ej, kx, ky, m, h, hl, sb0, sb1, src, slabs);
+            const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
+            st_vec(H + 3 * cell0, h);
+            if constexpr (P::COMP) st_vec(Hlo + 3 * cell0, hl);
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        if (issued < nfill) {
+            if (ty == 0) {
+                fence_proxy_async();
+                issue(issued);
+            }
+            ++issued;
+        }
+    }
+    if (abort_flag && tid == 0) {
+        atomicOr(g.status, 1);
+        for (int q = r; q < issued; ++q) mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1));
+    }
+}
+
+}  // namespace fdtd

@@ -68,6 +68,8 @@ class Engine:
     def __init__(self, grid, x_chunk=0):
         self.grid = grid
         self.x_chunk = x_chunk
+        # fused-pass kernel choice: variant 0 auto / 1 register streaming / 2 TMA-staged
+        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0}
         self.plan = None
         self._key = None
         self._keep = []
@@ -86,8 +88,8 @@ class Engine:
     # --- plan -------------------------------------------------------------------
     def _state_key(self):
         g = self.grid
-        return (tuple(o._coef_key() for o in g.objects), self.x_chunk, g.courant_number,
-                g._E.data_ptr(), g._H.data_ptr())
+        return (tuple(o._coef_key() for o in g.objects), self.x_chunk, tuple(sorted(self.tuning.items())),
+                g.courant_number, g._E.data_ptr(), g._H.data_ptr())
 
     def refresh(self):
         g = self.grid
@@ -102,12 +104,34 @@ class Engine:
         self.x_chunk = int(x_chunk)
         self.refresh()
 
+    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None):
+        """Choose the fused-pass kernels (0 auto, 1 register streaming, 2 TMA-staged),
+        the TMA tile rows (4 or 8) and ring stages; 0 keeps the automatic choice."""
+        for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages)):
+            if v is not None:
+                self.tuning[k] = int(v)
+        if x_chunk is not None:
+            self.x_chunk = int(x_chunk)
+        self.refresh()
+
     def tiling(self):
-        """(cells per thread along z, threads along z, rows per CTA, planes per
-        CTA along x, CTAs, kernel launches per step)."""
-        out = (ctypes.c_int64 * 6)()
+        """dict of the launch shape the plan chose."""
+        out = (ctypes.c_int64 * 8)()
         _native.check(_native.load().fdtd_plan_tiling(self.plan, out), "fdtd_plan_tiling")
-        return tuple(out)
+        keys = ("cells_per_thread_z", "threads_z", "rows_y", "planes_x", "ctas", "launches_per_step",
+                "variant", "stages")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def check_status(self):
+        """Raise RuntimeError if a staged kernel reported a pipeline failure."""
+        lib = _native.load()
+        st = ctypes.c_int32(0)
+        stream = torch.cuda.current_stream(self.grid._device).cuda_stream
+        _native.check(lib.fdtd_plan_status(self.plan, ctypes.byref(st), 1, ctypes.c_void_p(stream)),
+                      "fdtd_plan_status")
+        if st.value != 0:
+            raise RuntimeError(f"fdtd kernel reported failure status {st.value}; results of the last run are "
+                               "invalid")
 
     def _freeze_traces(self):
         for det, (p0, p1) in self.det_ranges.items():
@@ -145,6 +169,9 @@ class Engine:
         d.precision = _PRECISION[g.precision]
         d.nx, d.ny, d.nz = g.Nx, g.Ny, g.Nz
         d.x_chunk = self.x_chunk
+        d.variant = self.tuning["variant"]
+        d.tile_rows = self.tuning["tile_rows"]
+        d.stages = self.tuning["stages"]
         d.courant = g.courant_number
         d.E, d.H = g._E.data_ptr(), g._H.data_ptr()
         d.E_lo = g._E_lo.data_ptr() if g._E_lo is not None else None
@@ -160,7 +187,7 @@ class Engine:
                 bd_.kind = _native.BOUNDARY_PML
                 bd_.axis, bd_.high, bd_.thickness = b.axis, b.high, b.thickness
                 for name in ("psi_E", "psi_H", "b_E", "c_E", "b_H", "c_H"):
-                    t = getattr(b, name)
+                    t = getattr(b, "_" + name if name.startswith("psi") else name)
                     if t.dtype != dt or not t.is_contiguous() or t.device.type != "cuda":
                         raise RuntimeError(f"PML {name} must be a contiguous {dt} CUDA tensor")
                     setattr(bd_, name, t.data_ptr())
@@ -244,7 +271,7 @@ class Engine:
         _native.check(lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan)), "fdtd_plan_create")
         self.plan = plan
         self._keep = keep
-        self.launches_per_step = self.tiling()[5]
+        self.launches_per_step = self.tiling()["launches_per_step"]
 
     # --- traces ---------------------------------------------------------------
     def _ensure_capacity(self, need):
@@ -338,4 +365,5 @@ class Engine:
         _native.check(lib.fdtd_field_stats(self.plan, out.data_ptr(), scratch.data_ptr(), ctypes.c_void_p(stream)),
                       "fdtd_field_stats")
         v = out.cpu().tolist()
+        self.check_status()
         return {"sum_E2": v[0], "sum_H2": v[1], "max_abs_E": v[2], "max_abs_H": v[3], "nonfinite": int(v[4])}

@@ -229,6 +229,7 @@ class Grid:
                 bar = None
         if bar is None:
             eng.run(n)
+            eng.check_status()
             return
         chunk = max(1, n // 100)
         done = 0
@@ -238,6 +239,7 @@ class Grid:
             done += m
             bar.update(m)
         bar.close()
+        eng.check_status()
 
     def step(self):
         """One E half step, one H half step, then time_steps_passed += 1."""

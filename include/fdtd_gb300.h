@@ -64,7 +64,9 @@ typedef enum { FDTD_BOUNDARY_PML = 0, FDTD_BOUNDARY_PERIODIC = 1 } fdtd_boundary
  * fdtd/boundaries.py:490-625.  Only the two auxiliaries per half step that
  * can be non-zero are stored (compact layout): psi_E holds, for every slab
  * cell, the pair (psi driving E[(axis+1)%3], psi driving E[(axis+2)%3]); the
- * slab cells are ordered like the grid with the slab axis cut to `thickness`.
+ * slab cells are ordered like the grid with the slab axis cut to `thickness`
+ * (for a z slab the stored z extent is thickness rounded up to even, so that
+ * every row of auxiliaries is a multiple of 16 bytes).
  * Periodic: replaces _PeriodicBoundary{X,Y,Z}.update_E/H
  * (fdtd/boundaries.py:184-219). */
 typedef struct {
@@ -120,7 +122,12 @@ typedef struct {
     int32_t abi_version;  /* FDTD_ABI_VERSION */
     int32_t precision;    /* fdtd_precision */
     int32_t nx, ny, nz;
-    int32_t x_chunk;      /* cells per CTA along x; 0 = automatic */
+    int32_t x_chunk;      /* planes per CTA along x; 0 = automatic */
+    int32_t variant;      /* fused-pass kernels: 0 automatic, 1 register streaming,
+                             2 TMA-staged (needs nz a multiple of 4 floats / 2 doubles) */
+    int32_t tile_rows;    /* TMA-staged: rows per CTA, 4 or 8; 0 = automatic */
+    int32_t stages;       /* TMA-staged: shared-memory ring depth, >= 2; 0 = automatic */
+    int32_t reserved;
     double courant;
     void *E;              /* [nx][ny][nz][3] */
     void *H;
@@ -168,6 +175,12 @@ int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out);
 /* Release the plan's own tables (never the caller's buffers). */
 int fdtd_plan_destroy(fdtd_plan *plan);
 
+/* Device status word of the plan, copied to *out after synchronising the
+ * stream: 0 = healthy; bit 0 = a staged kernel's pipeline wait expired (the
+ * step's results are invalid).  reset != 0 clears the word afterwards.  No
+ * reference counterpart (the reference cannot fail this way). */
+int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t stream);
+
 /* Grid.run / Grid.step / Grid.update_E / Grid.update_H
  * (fdtd/grid.py:250-325): n_steps steps (or one half step) with detector
  * sampling and DFT accumulation after each half step. */
@@ -189,10 +202,10 @@ int fdtd_curl_H(int32_t precision, const void *H, void *out, int32_t nx, int32_t
 size_t fdtd_stats_scratch_bytes(const fdtd_plan *plan);
 int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_stream_t stream);
 
-/* Launch tiling chosen by the plan: out[0..5] = cells per thread along z,
- * threads along z, rows along y, cells along x per CTA, CTAs, kernels per
- * full step. */
-int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out6);
+/* Launch tiling chosen by the plan: out[0..7] = cells per thread along z,
+ * threads along z, rows along y, planes along x per CTA, CTAs, kernels per
+ * full step, variant (1 register streaming, 2 TMA-staged), ring stages. */
+int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8);
 
 const char *fdtd_status_string(int32_t status);
 int32_t fdtd_last_cuda_error(void);

@@ -158,17 +158,57 @@ def test_run_step_and_halves_agree(fd):
         assert np.array_equal(np.asarray(a.detector.E), np.asarray(g.detector.E))
 
 
+TILINGS = [dict(variant=1, x_chunk=1), dict(variant=1, x_chunk=7), dict(variant=2, tile_rows=8, stages=2),
+           dict(variant=2, tile_rows=4, stages=3, x_chunk=5), dict(variant=2, tile_rows=8, stages=3, x_chunk=24)]
+
+
 @pytest.mark.parametrize("prec", ["float64", "float32", "float32c"])
-def test_tiling_does_not_change_results(fd, prec):
+def test_kernel_variants_and_tiling_agree_bitwise(fd, prec):
+    """Register-streaming and TMA-staged kernels, any tile shape and ring depth,
+    give identical bits (same per-cell arithmetic, only the data path differs)."""
     fd.set_backend("gb300." + prec)
     build, _ = SCENES["c2_n24"]
     ref = build(fd)
+    ref._ensure_engine().set_tuning(variant=1)
     ref.run(20, progress_bar=False)
-    for chunk in (1, 3, 7, 24):
+    for tune in TILINGS:
         g = build(fd)
-        g._ensure_engine().set_x_chunk(chunk)
+        g._ensure_engine().set_tuning(**tune)
+        assert g._engine.tiling()["variant"] == tune["variant"]
         g.run(20, progress_bar=False)
-        assert torch.equal(g.E, ref.E) and torch.equal(g.H, ref.H), chunk
+        assert torch.equal(g.E, ref.E) and torch.equal(g.H, ref.H), tune
+        assert np.array_equal(np.asarray(g.detector.E), np.asarray(ref.detector.E)), tune
+
+
+@pytest.mark.parametrize("prec", ["float64", "float32"])
+def test_tma_variant_on_wide_grid_against_oracle(fd, prec):
+    """A grid wider than one TMA tile along z and y (several CTAs, tile edges,
+    periodic x, PML on y/z, objects crossing tile borders)."""
+    fd.set_backend("gb300." + prec)
+    from fdtd_gb300 import scenes
+
+    def build(mod):
+        g = mod.Grid((20, 36, 136), grid_spacing=155e-9, permittivity=scenes.c3_permittivity(36, seed=9)[:20, :, :1]
+                     * np.ones((1, 1, 136)))
+        g[:, 0:4, :] = mod.PML()
+        g[:, -3:, :] = mod.PML()
+        g[:, :, 0:5] = mod.PML()
+        g[:, :, -4:] = mod.PML()
+        g[0, :, :] = mod.PeriodicBoundary()
+        g[5:15, 6:30, 100:132] = mod.Object(permittivity=3.0)
+        g[3:12, 10:20, 60:70] = mod.AbsorbingObject(permittivity=2.0, conductivity=2e4)
+        g[10, 18, 68] = mod.PointSource(period=13)
+        g[:, 18, 60] = mod.LineDetector()
+        return g
+
+    g, o = build(fd), build(fo)
+    g._ensure_engine().set_tuning(variant=2)
+    assert g._engine.tiling()["variant"] == 2
+    g.run(40, progress_bar=False)
+    o.run(40)
+    tol = TOL64 if prec == "float64" else TOL32
+    assert rel_l2(g.E, o.E) <= tol and rel_l2(g.H, o.H) <= tol
+    assert rel_l2(np.asarray(g.detectors[0].E), np.stack(o.detectors[0].E)) <= tol
 
 
 def test_records_survive_plan_rebuild(fd):
