@@ -60,6 +60,20 @@ def test_float64_matches_reference_golden(fd, name):
     _compare(golden_scenes.snapshot(grid), ref, TOL64, name)
 
 
+@pytest.mark.parametrize("name", sorted(set(golden_scenes.SCENES) - {"mix"}))
+def test_float64_bit_identical_to_reference(fd, name):
+    """Same operation order as the reference: identical bits on every fixture
+    without an anisotropic object (the "mix" scene has one)."""
+    fd.set_backend("gb300.float64")
+    grid, steps, drive = golden_scenes.SCENES[name](fd)
+    drive(grid, steps)
+    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    snap = golden_scenes.snapshot(grid)
+    for key in ref.files:
+        if key != "steps":
+            assert np.array_equal(snap[key], ref[key]), f"{name}:{key} max |diff| {np.abs(snap[key] - ref[key]).max()}"
+
+
 @pytest.mark.parametrize("prec", ["float32", "float32c"])
 @pytest.mark.parametrize("name", sorted(golden_scenes.SCENES))
 def test_float32_close_to_reference_golden(fd, prec, name):
