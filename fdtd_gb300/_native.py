@@ -17,6 +17,7 @@ MAX_BOUNDARIES = 9
 FLOAT32, FLOAT32C, FLOAT64 = 0, 1, 2
 BOUNDARY_PML, BOUNDARY_PERIODIC = 0, 1
 ITEM_OBJECT, ITEM_ABSORBING, ITEM_ANISOTROPIC, ITEM_SOFT, ITEM_HARD = 0, 1, 2, 3, 4
+STATS_STATIC_MAX_ROWS = 1024  # FDTD_STATS_STATIC_MAX_ROWS
 
 STATUS = {
     0: "ok",
@@ -96,6 +97,7 @@ SIGNATURES = {
     "fdtd_curl_H": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p]),
     "fdtd_stats_scratch_bytes": (ctypes.c_size_t, [c_void_p]),
     "fdtd_field_stats": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fdtd_field_stats_noalloc": (c_int32, [c_void_p, c_void_p, c_int32, c_void_p]),
     "fdtd_plan_tiling": (c_int32, [c_void_p, ctypes.POINTER(c_int64)]),
     "fdtd_status_string": (ctypes.c_char_p, [c_int32]),
     "fdtd_last_cuda_error": (c_int32, []),

@@ -3,6 +3,7 @@
 // dispatch to the per-precision launch sequences.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "fdtd_kernels.cuh"
@@ -580,6 +581,64 @@ int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_s
         k_stats_partial<float, false><<<p.stats_ctas, kThreads, 0, st>>>((const float *)g.E, nullptr,
                                                                          (const float *)g.H, nullptr, nvals, part);
     k_stats_final<<<1, 32, 0, st>>>(part, p.stats_ctas, stats);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
+}
+
+}  // extern "C"
+
+// Partial sums of fdtd_field_stats_noalloc: a fixed array in device memory,
+// one copy per GPU that loads the library.  Host code must not use the
+// symbol itself as a device address (it is a host-side stand-in); its device
+// address is looked up once per device with cudaGetSymbolAddress.
+static __device__ __align__(256) double g_stats_rows[FDTD_STATS_STATIC_MAX_ROWS * 5];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_rows_mutex;
+double *g_rows_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_stats_rows on the current device (looked up on first use).
+int stats_rows_address(double **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (dev < 0 || dev >= kMaxDevices) return FDTD_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_rows_mutex);
+    if (g_rows_addr[dev] == nullptr) {
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_stats_rows);
+        if (e != cudaSuccess) return cuda_fail(e);
+        g_rows_addr[dev] = static_cast<double *>(ptr);
+    }
+    *out = g_rows_addr[dev];
+    return FDTD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_rows, fdtd_stream_t stream) {
+    if (!plan || !stats || n_rows < 0) return FDTD_ERR_ARGUMENT;
+    const Plan &p = plan->p;
+    const int rows = n_rows ? n_rows : p.stats_ctas;
+    if (rows > FDTD_STATS_STATIC_MAX_ROWS) return FDTD_ERR_RANGE;
+    double *part = nullptr;
+    const int rc = stats_rows_address(&part);
+    if (rc != FDTD_OK) return rc;
+    const GridK &g = p.k;
+    const long nvals = 3L * g.nx * g.ny * g.nz;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (p.precision == FDTD_FLOAT64)
+        k_stats_partial<double, false><<<rows, kThreads, 0, st>>>((const double *)g.E, nullptr,
+                                                                 (const double *)g.H, nullptr, nvals, part);
+    else if (p.precision == FDTD_FLOAT32C)
+        k_stats_partial<float, true><<<rows, kThreads, 0, st>>>((const float *)g.E, (const float *)g.Elo,
+                                                               (const float *)g.H, (const float *)g.Hlo, nvals, part);
+    else
+        k_stats_partial<float, false><<<rows, kThreads, 0, st>>>((const float *)g.E, nullptr, (const float *)g.H,
+                                                                nullptr, nvals, part);
+    k_stats_final<<<1, 32, 0, st>>>(part, rows, stats);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
 }

@@ -202,6 +202,26 @@ int fdtd_curl_H(int32_t precision, const void *H, void *out, int32_t nx, int32_t
 size_t fdtd_stats_scratch_bytes(const fdtd_plan *plan);
 int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_stream_t stream);
 
+/* fdtd_field_stats without any device allocation, for callers that cannot
+ * call cudaMalloc or hand out a scratch buffer: for example a host
+ * application whose device memory is owned by another framework's allocator,
+ * or a monitoring hook between time steps that must not touch an allocator
+ * (cudaMalloc/cudaFree can synchronise the device and fragment a caching
+ * allocator).  The per-CTA partial sums live in a fixed device array compiled
+ * into this library: FDTD_STATS_STATIC_MAX_ROWS rows of 5 doubles (40 KiB),
+ * held by every GPU that loads the library until the process exits.
+ * n_rows = number of partial rows (CTAs) to use, 0 = the plan's default (the
+ * same rows fdtd_field_stats uses, so both give identical results); a value
+ * above FDTD_STATS_STATIC_MAX_ROWS returns FDTD_ERR_RANGE without launching.
+ * The first call on a device looks up the array's device address (with that
+ * device current) and keeps it; make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's contents
+ * (every row used is rewritten before it is read, so nothing needs clearing);
+ * calls that overlap on the GPU race with each other.  No counterpart in the
+ * reference (the reference has no health check). */
+#define FDTD_STATS_STATIC_MAX_ROWS 1024
+int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_rows, fdtd_stream_t stream);
+
 /* Launch tiling chosen by the plan: out[0..7] = cells per thread along z,
  * threads along z, rows along y, planes along x per CTA, CTAs, kernels per
  * full step, variant (1 register streaming, 2 TMA-staged), ring stages. */
