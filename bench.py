@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--n", type=int, default=768, help="grid edge (config 3 is 768)")
+    p.add_argument("--pml", type=int, default=-1, help="PML cells on y and z (default 20 scaled by n/768; 0 = none)")
     p.add_argument("--x-chunk", type=int, default=0, help="planes per CTA along x (0 = plan default)")
     p.add_argument("--variant", type=int, default=0, help="0 auto, 1 register streaming, 2 TMA-staged")
     p.add_argument("--tile-rows", type=int, default=0)
@@ -190,7 +191,7 @@ def traffic_from_profile(precision, n):
 
 def build_grid(fd, scenes, prec, n, eps, args):
     fd.set_backend("gb300." + prec)
-    pml = max(2, int(round(20 * n / 768)))
+    pml = max(2, int(round(20 * n / 768))) if args.pml < 0 else args.pml
     g = scenes.c3(fd, n=n, pml=pml, eps=eps, detector=True)
     eng = g._ensure_engine()
     eng.set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages, x_chunk=args.x_chunk)
@@ -343,6 +344,7 @@ def gb300_arm(args):
             "grid": [n, n, n],
             "geometry": "400 random blocks eps in {1,2.25,12.1}, PML y/z, periodic x, centre point source, "
                         "line detector",
+            "pml": max(2, int(round(20 * n / 768))) if args.pml < 0 else args.pml,
             "l2": "inputs larger than L2 (fields + materials >= 22 GB at 768^3); no flush",
             "parallelism": "replicas" if dist.world > 1 else "single GPU",
         },

@@ -130,8 +130,9 @@ class Object:
         return coefs
 
     def _make_coefficients(self, dtype):
-        ci = self.grid.courant_number * self._inverse_permittivity
-        return [ci.to(dtype).contiguous()]
+        # host float64 arithmetic: elementwise IEEE results identical to numpy's
+        ci = self.grid.courant_number * self._inverse_permittivity.cpu()
+        return [ci.to(dtype).to(self.grid._device).contiguous()]
 
     def __repr__(self):
         return f"{self.__class__.__name__}(name={repr(self.name)})"
@@ -166,8 +167,9 @@ class AbsorbingObject(Object):
 
     def _after_update(self):
         g = self.grid
-        self.absorption_factor = (0.5 * g.courant_number * self._inverse_permittivity * self.conductivity
-                                  * g.grid_spacing * const.eta0)
+        f = (0.5 * g.courant_number * self._inverse_permittivity.cpu() * self.conductivity.cpu()
+             * g.grid_spacing * const.eta0)
+        self.absorption_factor = f.to(g._device)
 
     def _coef_key(self):
         ie, cond = self._inverse_permittivity, self.conductivity
@@ -175,13 +177,15 @@ class AbsorbingObject(Object):
 
     def _make_coefficients(self, dtype):
         self._after_update()
-        f = self.absorption_factor
+        # host float64 arithmetic: elementwise IEEE results identical to numpy's
+        f = self.absorption_factor.cpu()
         r = (1 - f) / (1 + f)
-        ci = self.grid.courant_number * self._inverse_permittivity
+        ci = self.grid.courant_number * self._inverse_permittivity.cpu()
         opf = 1 + f
+        dev = self.grid._device
         if dtype == torch.float64:
-            return [r.contiguous(), ci.contiguous(), opf.contiguous()]
-        return [r.to(dtype).contiguous(), (ci / opf).to(dtype).contiguous()]
+            return [r.contiguous().to(dev), ci.contiguous().to(dev), opf.contiguous().to(dev)]
+        return [r.to(dtype).contiguous().to(dev), (ci / opf).to(dtype).contiguous().to(dev)]
 
 
 class AnisotropicObject(Object):

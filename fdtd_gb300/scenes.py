@@ -108,10 +108,11 @@ def c3(fd, n=768, pml=20, seed=3, periodic_first=False, eps=None, detector=False
     grid = fd.Grid((n, n, n), grid_spacing=SPACING, permittivity=eps, permeability=1.0)
     if periodic_first:
         grid[0, :, :] = fd.PeriodicBoundary(name="xbounds")
-    grid[:, 0:pml, :] = fd.PML(name="pml_ylow")
-    grid[:, -pml:, :] = fd.PML(name="pml_yhigh")
-    grid[:, :, 0:pml] = fd.PML(name="pml_zlow")
-    grid[:, :, -pml:] = fd.PML(name="pml_zhigh")
+    if pml:
+        grid[:, 0:pml, :] = fd.PML(name="pml_ylow")
+        grid[:, -pml:, :] = fd.PML(name="pml_yhigh")
+        grid[:, :, 0:pml] = fd.PML(name="pml_zlow")
+        grid[:, :, -pml:] = fd.PML(name="pml_zhigh")
     if not periodic_first:
         grid[0, :, :] = fd.PeriodicBoundary(name="xbounds")
     c = n // 2

@@ -61,17 +61,20 @@ def test_float64_matches_reference_golden(fd, name):
 
 
 @pytest.mark.parametrize("name", sorted(set(golden_scenes.SCENES) - {"mix"}))
-def test_float64_bit_identical_to_reference(fd, name):
-    """Same operation order as the reference: identical bits on every fixture
-    without an anisotropic object (the "mix" scene has one)."""
+def test_float64_bit_identical_to_reference_arithmetic(fd, name):
+    """Same operation order as the reference: identical bits to the oracle run
+    on this host (the oracle is bit-identical to the reference, see
+    test_oracle_golden.py) on every golden scene without an anisotropic object.
+    Compared on the same host because numpy's exp, used at registration and by
+    the "manual" scene's driver, can differ in the last bit between machines."""
     fd.set_backend("gb300.float64")
     grid, steps, drive = golden_scenes.SCENES[name](fd)
     drive(grid, steps)
-    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
-    snap = golden_scenes.snapshot(grid)
-    for key in ref.files:
-        if key != "steps":
-            assert np.array_equal(snap[key], ref[key]), f"{name}:{key} max |diff| {np.abs(snap[key] - ref[key]).max()}"
+    ogrid, _, odrive = golden_scenes.SCENES[name](fo)
+    odrive(ogrid, steps)
+    snap, ref = golden_scenes.snapshot(grid), golden_scenes.snapshot(ogrid)
+    for key, val in ref.items():
+        assert np.array_equal(snap[key], val), f"{name}:{key} max |diff| {np.abs(snap[key] - val).max()}"
 
 
 @pytest.mark.parametrize("prec", ["float32", "float32c"])
