@@ -11,6 +11,9 @@ kernel pass through the C ABI in include/fdtd_gb300.h.
     grid[0:10, :, :] = fdtd.PML(name="pml_xlow")
     ...
     grid.run(500)
+
+Gradients with respect to design objects' inverse permittivity come from a
+reverse-time adjoint behind torch.autograd (``fdtd_gb300.adjoint.run``).
 """
 
 __version__ = "0.1.0"
@@ -21,11 +24,11 @@ from .detectors import BlockDetector, CurrentDetector, DFTPlaneDetector, LineDet
 from .grid import Grid
 from .objects import AbsorbingObject, AnisotropicObject, Object
 from .sources import GaussianPlaneSource, LineSource, PlaneSource, PointSource, SoftArbitraryPointSource
-from . import constants, waveforms, conversions
+from . import adjoint, constants, waveforms, conversions
 
 __all__ = [
     "Grid", "PML", "PeriodicBoundary", "DomainBorderPML", "Object", "AbsorbingObject",
     "AnisotropicObject", "PointSource", "LineSource", "PlaneSource", "GaussianPlaneSource",
     "SoftArbitraryPointSource", "LineDetector", "BlockDetector", "CurrentDetector", "PlaneDetector",
-    "DFTPlaneDetector", "backend", "set_backend", "constants", "waveforms", "conversions",
+    "DFTPlaneDetector", "backend", "set_backend", "adjoint", "constants", "waveforms", "conversions",
 ]

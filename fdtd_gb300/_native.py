@@ -87,12 +87,33 @@ class RunArgs(ctypes.Structure):
     ]
 
 
+class CaptureArgs(ctypes.Structure):
+    _fields_ = [
+        ("detectors", c_int32), ("n_curl", c_int32),
+        ("curl", ctypes.POINTER(c_void_p)),
+    ]
+
+
+class AdjointArgs(ctypes.Structure):
+    _fields_ = [
+        ("n_steps", c_int64), ("parity", c_int32), ("n_objects", c_int32),
+        ("lam_E", c_void_p), ("lam_H", c_void_p),
+        ("aux_E", (c_void_p * 2) * MAX_BOUNDARIES), ("aux_H", (c_void_p * 2) * MAX_BOUNDARIES),
+        ("seed_E", c_void_p), ("seed_H", c_void_p), ("seed_row", c_int64),
+        ("dft_grad", ctypes.POINTER(c_void_p)), ("phase", c_void_p),
+        ("curl", ctypes.POINTER(c_void_p)), ("curl_row", c_int64),
+        ("grad", ctypes.POINTER(c_void_p)),
+    ]
+
+
 # every symbol declared in include/fdtd_gb300.h with (restype, argtypes)
 SIGNATURES = {
     "fdtd_plan_create": (c_int32, [ctypes.POINTER(GridDesc), ctypes.POINTER(c_void_p)]),
     "fdtd_plan_destroy": (c_int32, [c_void_p]),
     "fdtd_plan_status": (c_int32, [c_void_p, ctypes.POINTER(c_int32), c_int32, c_void_p]),
     "fdtd_run": (c_int32, [c_void_p, ctypes.POINTER(RunArgs), c_void_p]),
+    "fdtd_run_capture": (c_int32, [c_void_p, ctypes.POINTER(RunArgs), ctypes.POINTER(CaptureArgs), c_void_p]),
+    "fdtd_adjoint_run": (c_int32, [c_void_p, ctypes.POINTER(AdjointArgs), c_void_p]),
     "fdtd_curl_E": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p]),
     "fdtd_curl_H": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p]),
     "fdtd_stats_scratch_bytes": (ctypes.c_size_t, [c_void_p]),

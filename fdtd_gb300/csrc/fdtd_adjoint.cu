@@ -1,0 +1,154 @@
+// Launch sequence of the reverse-time adjoint (fdtd_adjoint_run), float32 and
+// float64 instantiations.
+#include "fdtd_adjoint.cuh"
+#include "fdtd_plan.hpp"
+
+namespace fdtd {
+
+static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
+
+static long box_cells(const ItemK &o) {
+    return (long)(o.hi[0] - o.lo[0]) * (o.hi[1] - o.lo[1]) * (o.hi[2] - o.lo[2]);
+}
+
+static int validate(const Plan &p, const fdtd_adjoint_args *a) {
+    if (a->n_steps < 0 || (a->parity != 0 && a->parity != 1)) return FDTD_ERR_ARGUMENT;
+    if (!a->lam_E || !a->lam_H) return FDTD_ERR_ARGUMENT;
+    if (p.adj_V > 1 && (!aligned16(a->lam_E) || !aligned16(a->lam_H))) return FDTD_ERR_ARGUMENT;
+    if ((a->curl || a->grad) && a->n_objects != p.n_objects) return FDTD_ERR_ARGUMENT;
+    for (int s = 0; s < p.k.nslab; ++s) {
+        const int b = p.slab_boundary[s];
+        for (int q = 0; q < 2; ++q)
+            if (!a->aux_E[b][q] || !a->aux_H[b][q]) return FDTD_ERR_ARGUMENT;
+    }
+    if (a->n_steps == 0) return FDTD_OK;
+    if ((a->seed_E || a->seed_H) && (p.n_probe == 0 || a->seed_row - (a->n_steps - 1) < 0))
+        return FDTD_ERR_RANGE;
+    bool any_dft = false;
+    if (a->dft_grad)
+        for (size_t q = 0; q < p.dft.size(); ++q) any_dft |= a->dft_grad[q] != nullptr;
+    if (any_dft && !a->phase) return FDTD_ERR_ARGUMENT;
+    if (a->grad) {
+        for (int q = 0; q < p.n_objects; ++q) {
+            if (!a->grad[q]) continue;
+            const int kind = p.items_host[q].kind;
+            if (kind != FDTD_ITEM_OBJECT && kind != FDTD_ITEM_ANISOTROPIC) return FDTD_ERR_UNSUPPORTED;
+            if (!a->curl || !a->curl[q]) return FDTD_ERR_ARGUMENT;
+            if (a->curl_row - (a->n_steps - 1) < 0) return FDTD_ERR_RANGE;
+        }
+    }
+    return FDTD_OK;
+}
+
+template <class T, int V>
+static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
+    GridK g = p.k;
+    g.E = a->lam_E;
+    g.H = a->lam_H;
+    g.Elo = g.Hlo = nullptr;
+    g.TZ = p.adj_TZ;
+    g.TY = p.adj_TY;
+    g.XC = p.adj_XC;
+    T *LE = (T *)a->lam_E;
+    T *LH = (T *)a->lam_H;
+    const int pblocks = (3 * p.n_probe + kThreads - 1) / kThreads;
+    int par = a->parity;
+    for (int64_t s = 0; s < a->n_steps; ++s) {
+        AdjAux x{};
+        for (int q = 0; q < g.nslab; ++q) {
+            const int b = p.slab_boundary[q];
+            x.Eo[q] = a->aux_E[b][par];
+            x.En[q] = a->aux_E[b][par ^ 1];
+            x.Ho[q] = a->aux_H[b][par];
+            x.Hn[q] = a->aux_H[b][par ^ 1];
+        }
+        const int64_t srow = a->seed_row - s, crow = a->curl_row - s;
+
+        // transposed H half: detectors, sources, boundaries after the first
+        // periodic one (reverse order), then the fused pass
+        if (a->seed_H && p.n_probe)
+            k_adj_seed_probe<T><<<pblocks, kThreads, 0, st>>>(LH, p.probe_cells, p.n_probe,
+                                                              (const T *)a->seed_H + srow * 3 * p.n_probe);
+        for (int q = p.srcH0; q < p.srcH0 + p.n_srcH; ++q)
+            if (p.items_host[q].kind == FDTD_ITEM_HARD)
+                k_adj_zero_box<T><<<grid_stride_blocks(box_cells(p.items_host[q])), kThreads, 0, st>>>(g, q, LH);
+        for (const EpiOp &op : p.adj_H) {
+            if (op.kind == EPI_COPY) {
+                const int n = op.axis == 0 ? g.nx : (op.axis == 1 ? g.ny : g.nz);
+                const int n1 = op.axis == 0 ? g.ny : g.nx, n2 = op.axis == 2 ? g.ny : g.nz;
+                k_adj_periodic<T><<<grid_stride_blocks((long)n1 * n2 * 3), kThreads, 0, st>>>(LH, g.nx, g.ny, g.nz,
+                                                                                           op.axis, n - 1, 0);
+            } else {
+                const SlabK &S = g.slab[op.slab];
+                const long cells = (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) *
+                                   (S.axis == 2 ? S.th : g.nz);
+                k_adj_slab_inc<T, false><<<grid_stride_blocks(cells), kThreads, 0, st>>>(
+                    g, op.slab, (T *)a->aux_H[p.slab_boundary[op.slab]][par]);
+            }
+        }
+        k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(g, x);
+
+        // transposed E half
+        if (a->seed_E && p.n_probe)
+            k_adj_seed_probe<T><<<pblocks, kThreads, 0, st>>>(LE, p.probe_cells, p.n_probe,
+                                                              (const T *)a->seed_E + srow * 3 * p.n_probe);
+        if (a->dft_grad) {
+            for (size_t q = 0; q < p.dft.size(); ++q) {
+                if (!a->dft_grad[q]) continue;
+                const fdtd_dft_desc &d = p.dft[q];
+                const long cells = (long)(d.hi[0] - d.lo[0]) * (d.hi[1] - d.lo[1]) * (d.hi[2] - d.lo[2]);
+                k_adj_seed_dft<T><<<grid_stride_blocks(cells * 3), kThreads, 0, st>>>(
+                    LE, g.ny, g.nz, d, a->dft_grad[q], a->phase + s * 2 * p.n_phase_columns);
+            }
+        }
+        for (int q = p.srcE0; q < p.srcE0 + p.n_srcE; ++q)
+            if (p.items_host[q].kind == FDTD_ITEM_HARD)
+                k_adj_zero_box<T><<<grid_stride_blocks(box_cells(p.items_host[q])), kThreads, 0, st>>>(g, q, LE);
+        for (const EpiOp &op : p.adj_E) {
+            if (op.kind == EPI_COPY) {
+                const int n = op.axis == 0 ? g.nx : (op.axis == 1 ? g.ny : g.nz);
+                const int n1 = op.axis == 0 ? g.ny : g.nx, n2 = op.axis == 2 ? g.ny : g.nz;
+                k_adj_periodic<T><<<grid_stride_blocks((long)n1 * n2 * 3), kThreads, 0, st>>>(LE, g.nx, g.ny, g.nz,
+                                                                                           op.axis, 0, n - 1);
+            } else {
+                const SlabK &S = g.slab[op.slab];
+                const long cells = (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) *
+                                   (S.axis == 2 ? S.th : g.nz);
+                k_adj_slab_inc<T, true><<<grid_stride_blocks(cells), kThreads, 0, st>>>(
+                    g, op.slab, (T *)a->aux_E[p.slab_boundary[op.slab]][par]);
+            }
+        }
+        k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(g, x);
+        for (int q = p.n_objects - 1; q >= 0; --q) {
+            const ItemK &o = p.items_host[q];
+            const long reach = (long)(o.hi[0] - std::max(0, o.lo[0] - 1)) * (o.hi[1] - std::max(0, o.lo[1] - 1)) *
+                               (o.hi[2] - std::max(0, o.lo[2] - 1));
+            double *gr = a->grad ? a->grad[q] : nullptr;
+            const T *cu = gr ? (const T *)a->curl[q] + crow * 3 * box_cells(o) : nullptr;
+            k_adj_object<T><<<grid_stride_blocks(reach), kThreads, 0, st>>>(g, q, cu, gr);
+            if (o.kind == FDTD_ITEM_ABSORBING)
+                k_adj_absorb_scale<T><<<grid_stride_blocks(3 * box_cells(o)), kThreads, 0, st>>>(g, q);
+        }
+        par ^= 1;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_last_cuda_error((int)e);
+            return FDTD_ERR_CUDA;
+        }
+    }
+    return FDTD_OK;
+}
+
+int adjoint_f32(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
+    const int rc = validate(p, a);
+    if (rc != FDTD_OK) return rc;
+    return p.adj_V == 4 ? adjoint_impl<float, 4>(p, a, st) : adjoint_impl<float, 1>(p, a, st);
+}
+
+int adjoint_f64(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
+    const int rc = validate(p, a);
+    if (rc != FDTD_OK) return rc;
+    return p.adj_V == 2 ? adjoint_impl<double, 2>(p, a, st) : adjoint_impl<double, 1>(p, a, st);
+}
+
+}  // namespace fdtd

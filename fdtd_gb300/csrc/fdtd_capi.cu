@@ -186,6 +186,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.epi_E.push_back(op);
         p.epi_H.push_back(op);
     }
+    // the adjoint undoes these boundary stages in reverse order
+    p.adj_E.assign(p.epi_E.rbegin(), p.epi_E.rend());
+    p.adj_H = p.adj_E;
+    for (int s = 0; s < g.nslab; ++s) p.slab_boundary[s] = slab_pos[s];
 
     // tiling
     int dev = 0, n_sm = 152, optin = 0;
@@ -297,6 +301,24 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     }
     t.gx = (d->nx + t.XC - 1) / t.XC;
     if (t.gx > 65535) return FDTD_ERR_UNSUPPORTED;
+    // adjoint kernels: register streaming, tiled like the register kernels
+    {
+        const int V = vec ? vmax : 1;
+        const int zt = (d->nz + V - 1) / V;
+        const int TZ = std::min(32, next_pow2(zt));
+        const int TY = kThreads / TZ;
+        const int gz = (zt + TZ - 1) / TZ, gy = (d->ny + TY - 1) / TY;
+        const long cols = (long)gz * gy, target = 4L * n_sm;
+        long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
+        chunks = std::max(1L, std::min(chunks, (long)d->nx));
+        const int XC = (int)((d->nx + chunks - 1) / chunks);
+        p.adj_V = V;
+        p.adj_TZ = TZ;
+        p.adj_TY = TY;
+        p.adj_XC = XC;
+        p.adj_grid = dim3(gz, gy, (d->nx + XC - 1) / XC);
+        p.adj_block = dim3(TZ, TY, 1);
+    }
     p.V = t.V;
     g.TZ = t.TZ;
     g.TY = t.TY;
@@ -347,6 +369,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     }
     const int srcH0 = srcE0 + d->n_sources_E;
     const int nitems = (int)items.size();
+    p.items_host = items;
+    p.n_objects = d->n_objects;
+    p.srcE0 = srcE0;
+    p.n_srcE = d->n_sources_E;
+    p.srcH0 = srcH0;
+    p.n_srcH = d->n_sources_H;
 
     // sources inside the fused pass unless a periodic copy must come first
     const std::vector<ItemK> &cit = items;
@@ -523,13 +551,40 @@ int fdtd_run(fdtd_plan *plan, const fdtd_run_args *args, fdtd_stream_t stream) {
     cudaStream_t st = (cudaStream_t)stream;
     switch (plan->p.precision) {
         case FDTD_FLOAT32:
-            return run_f32(plan->p, args, st);
+            return run_f32(plan->p, args, nullptr, st);
         case FDTD_FLOAT32C:
-            return run_f32c(plan->p, args, st);
+            return run_f32c(plan->p, args, nullptr, st);
         case FDTD_FLOAT64:
-            return run_f64(plan->p, args, st);
+            return run_f64(plan->p, args, nullptr, st);
     }
     return FDTD_ERR_ARGUMENT;
+}
+
+int fdtd_run_capture(fdtd_plan *plan, const fdtd_run_args *args, const fdtd_capture_args *cap,
+                     fdtd_stream_t stream) {
+    if (!plan || !args || !cap) return FDTD_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (plan->p.precision) {
+        case FDTD_FLOAT32:
+            return run_f32(plan->p, args, cap, st);
+        case FDTD_FLOAT32C:
+            return run_f32c(plan->p, args, cap, st);
+        case FDTD_FLOAT64:
+            return run_f64(plan->p, args, cap, st);
+    }
+    return FDTD_ERR_ARGUMENT;
+}
+
+int fdtd_adjoint_run(fdtd_plan *plan, const fdtd_adjoint_args *args, fdtd_stream_t stream) {
+    if (!plan || !args) return FDTD_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (plan->p.precision) {
+        case FDTD_FLOAT32:
+            return adjoint_f32(plan->p, args, st);
+        case FDTD_FLOAT64:
+            return adjoint_f64(plan->p, args, st);
+    }
+    return FDTD_ERR_UNSUPPORTED;
 }
 
 static int curl_common(int32_t precision, const void *in, void *out, int32_t nx, int32_t ny, int32_t nz,
@@ -689,6 +744,10 @@ size_t fdtd_abi_sizeof(int32_t which) {
             return sizeof(fdtd_dft_desc);
         case 4:
             return sizeof(fdtd_run_args);
+        case 5:
+            return sizeof(fdtd_capture_args);
+        case 6:
+            return sizeof(fdtd_adjoint_args);
     }
     return 0;
 }

@@ -2,7 +2,9 @@
 #include "fdtd_launch.cuh"
 
 namespace fdtd {
-int run_f64(Plan &p, const fdtd_run_args *a, cudaStream_t st) { return run_impl<PF64>(p, a, st); }
+int run_f64(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaStream_t st) {
+    return run_impl<PF64>(p, a, cap, st);
+}
 int prepare_tma_f64(Plan &p) { return prepare_tma_impl<PF64>(p); }
 
 size_t tma_stage_bytes(int precision, int tile_rows) {

@@ -3,6 +3,7 @@
 
 #include <cudaTypedefs.h>
 
+#include "fdtd_adjoint.cuh"
 #include "fdtd_kernels.cuh"
 #include "fdtd_plan.hpp"
 #include "fdtd_tma.cuh"
@@ -157,14 +158,24 @@ static size_t stage_bytes_of(int tile_rows) {
                           : (size_t)StageGeom<typename P::T, 4, P::COMP>::stageBytes;
 }
 
+// n_steps full steps (or one half step).  With capture arguments: detectors
+// and DFTs only when cap->detectors is set, and curl_H on every object box
+// with a capture pointer before each E half (reverse-time adjoint).
 template <class P>
-static int run_impl(Plan &p, const fdtd_run_args *a, cudaStream_t st) {
+static int run_impl(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaStream_t st) {
     using T = typename P::T;
     if (a->n_steps < 0 || (a->half != 0 && a->n_steps != 1) || a->half < 0 || a->half > 2)
         return FDTD_ERR_ARGUMENT;
+    if (cap != nullptr) {
+        if (a->half != 0 || (cap->n_curl != 0 && cap->n_curl != p.n_objects) ||
+            (cap->n_curl != 0 && cap->curl == nullptr))
+            return FDTD_ERR_ARGUMENT;
+    }
+    const bool detect = cap == nullptr || cap->detectors != 0;
     if (p.n_columns > 0 && a->wave == nullptr && a->n_steps > 0) return FDTD_ERR_ARGUMENT;
-    if (!p.dft.empty() && a->phase == nullptr && a->n_steps > 0 && a->half != 2) return FDTD_ERR_ARGUMENT;
-    const bool probe = p.n_probe > 0;
+    if (detect && !p.dft.empty() && a->phase == nullptr && a->n_steps > 0 && a->half != 2)
+        return FDTD_ERR_ARGUMENT;
+    const bool probe = detect && p.n_probe > 0;
     if (probe) {
         if (a->half != 2 && (a->trace_E == nullptr || a->record_E < 0 ||
                              a->record_E + a->n_steps > a->trace_capacity))
@@ -177,16 +188,27 @@ static int run_impl(Plan &p, const fdtd_run_args *a, cudaStream_t st) {
     const int pblocks = (3 * p.n_probe + kThreads - 1) / kThreads;
     for (int64_t s = 0; s < a->n_steps; ++s) {
         const double *wave = p.n_columns > 0 ? a->wave + s * p.n_columns : nullptr;
+        if (cap != nullptr) {
+            for (int q = 0; q < cap->n_curl; ++q) {
+                if (cap->curl[q] == nullptr) continue;
+                const ItemK &o = p.items_host[q];
+                const long cells = (long)(o.hi[0] - o.lo[0]) * (o.hi[1] - o.lo[1]) * (o.hi[2] - o.lo[2]);
+                k_capture_curl<T><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, q, (T *)cap->curl[q] +
+                                                                                          s * 3 * cells);
+            }
+        }
         if (a->half != 2) {
             launch_fused<P>(p, true, wave, st);
             launch_epilogue<P>(p, true, wave, st);
             if (probe)
                 k_probe<T><<<pblocks, kThreads, 0, st>>>((const T *)g.E, p.probe_cells, p.n_probe,
                                                         (T *)a->trace_E + (a->record_E + s) * 3 * p.n_probe);
-            for (const fdtd_dft_desc &d : p.dft) {
-                const long cells = (long)(d.hi[0] - d.lo[0]) * (d.hi[1] - d.lo[1]) * (d.hi[2] - d.lo[2]);
-                k_dft<T, P::COMP><<<grid_stride_blocks(cells * 3), kThreads, 0, st>>>(
-                    (const T *)g.E, (const T *)g.Elo, g.ny, g.nz, d, a->phase + s * 2 * p.n_phase_columns);
+            if (detect) {
+                for (const fdtd_dft_desc &d : p.dft) {
+                    const long cells = (long)(d.hi[0] - d.lo[0]) * (d.hi[1] - d.lo[1]) * (d.hi[2] - d.lo[2]);
+                    k_dft<T, P::COMP><<<grid_stride_blocks(cells * 3), kThreads, 0, st>>>(
+                        (const T *)g.E, (const T *)g.Elo, g.ny, g.nz, d, a->phase + s * 2 * p.n_phase_columns);
+                }
             }
         }
         if (a->half != 1) {

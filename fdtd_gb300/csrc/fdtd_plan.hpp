@@ -42,12 +42,26 @@ struct Plan {
     void *dev_mem;     // the plan's own device tables
     int stats_ctas;
     int launches_per_step;
+    // reverse-time adjoint: launch shape of k_adj_E / k_adj_H, host copies of
+    // the items (objects, then E sources, then H sources), the grid.boundaries
+    // index of every slab, and the periodic transposes / slab increments that
+    // precede the transposed fused pass, in reverse boundary order
+    int adj_V;
+    dim3 adj_grid, adj_block;
+    int adj_TZ, adj_TY, adj_XC;
+    std::vector<ItemK> items_host;
+    int n_objects, srcE0, n_srcE, srcH0, n_srcH;
+    int slab_boundary[kMaxSlabs];
+    std::vector<EpiOp> adj_E, adj_H;
 };
 
-// Per-precision entry points (one translation unit per precision).
-int run_f32(Plan &p, const fdtd_run_args *a, cudaStream_t st);
-int run_f32c(Plan &p, const fdtd_run_args *a, cudaStream_t st);
-int run_f64(Plan &p, const fdtd_run_args *a, cudaStream_t st);
+// Per-precision entry points (one translation unit per precision).  `cap`
+// may be null (plain fdtd_run).
+int run_f32(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaStream_t st);
+int run_f32c(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaStream_t st);
+int run_f64(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaStream_t st);
+int adjoint_f32(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st);
+int adjoint_f64(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st);
 
 // Stage size in bytes of the TMA-staged kernels for a precision and tile rows.
 size_t tma_stage_bytes(int precision, int tile_rows);

@@ -296,7 +296,25 @@ class Engine:
         return buf[:n, p0:p1, :].reshape((n,) + det._rec_shape)
 
     # --- stepping --------------------------------------------------------------
-    def _tables(self, q0, n):
+    def phase_table(self, steps):
+        """(len(steps), n_phase, 2) float64 numpy table of the DFT factors
+        (cos, -sin) of 2 pi f q dt for the step indices q in ``steps``."""
+        g = self.grid
+        ph = np.empty((len(steps), self.n_phase, 2), dtype=np.float64)
+        col = 0
+        for det in self.dfts:
+            for f in det.frequencies:
+                for r, q in enumerate(steps):
+                    theta = 2.0 * math.pi * f * (q * g.time_step)
+                    ph[r, col, 0] = math.cos(theta)
+                    ph[r, col, 1] = -math.sin(theta)
+                col += 1
+        return ph
+
+    def upload_phase(self, table):
+        return self._phase_stage.upload(table, self.grid._device)
+
+    def _tables(self, q0, n, dft=True):
         g = self.grid
         wave = phase = None
         if self.sources:
@@ -305,42 +323,54 @@ class Engine:
                 for r in range(n):
                     tab[r, c] = s._value(q0 + r)
             wave = self._wave_stage.upload(tab, g._device)
-        if self.n_phase:
-            ph = np.empty((n, self.n_phase, 2), dtype=np.float64)
-            col = 0
-            for det in self.dfts:
-                for f in det.frequencies:
-                    for r in range(n):
-                        theta = 2.0 * math.pi * f * ((q0 + r) * g.time_step)
-                        ph[r, col, 0] = math.cos(theta)
-                        ph[r, col, 1] = -math.sin(theta)
-                    col += 1
-            phase = self._phase_stage.upload(ph, g._device)
+        if self.n_phase and dft:
+            phase = self.upload_phase(self.phase_table(range(q0, q0 + n)))
         return wave, phase
 
-    def _launch(self, n, half):
+    def _launch(self, n, half, capture=None):
+        """fdtd_run, or with ``capture = (detectors, curls)`` fdtd_run_capture
+        (curls: per object a device tensor of n rows or None)."""
         g = self.grid
         lib = _native.load()
         q0 = g.time_steps_passed
-        wave, phase = self._tables(q0, n)
+        detect = capture is None or capture[0]
+        wave, phase = self._tables(q0, n, dft=detect)
         a = _native.RunArgs()
         a.n_steps, a.half = n, half
         a.wave = wave.data_ptr() if wave is not None else None
         a.phase = phase.data_ptr() if phase is not None else None
-        if self.n_probe:
+        if self.n_probe and detect:
             need_E = self.rec_E + (n if half != 2 else 0)
             need_H = self.rec_H + (n if half != 1 else 0)
             self._ensure_capacity(max(need_E, need_H))
             a.trace_E, a.trace_H = self.trace_E.data_ptr(), self.trace_H.data_ptr()
             a.trace_capacity = self.capacity
             a.record_E, a.record_H = self.rec_E, self.rec_H
-        stream = torch.cuda.current_stream(g._device).cuda_stream
-        _native.check(lib.fdtd_run(self.plan, ctypes.byref(a), ctypes.c_void_p(stream)), "fdtd_run")
-        if self.n_probe:
+        stream = ctypes.c_void_p(torch.cuda.current_stream(g._device).cuda_stream)
+        if capture is None:
+            _native.check(lib.fdtd_run(self.plan, ctypes.byref(a), stream), "fdtd_run")
+        else:
+            curls = capture[1]
+            c = _native.CaptureArgs()
+            c.detectors = 1 if detect else 0
+            c.n_curl = len(curls)
+            arr = (ctypes.c_void_p * max(1, len(curls)))(*[_native.ptr(t) for t in curls])
+            c.curl = arr
+            _native.check(lib.fdtd_run_capture(self.plan, ctypes.byref(a), ctypes.byref(c), stream),
+                          "fdtd_run_capture")
+        if self.n_probe and detect:
             if half != 2:
                 self.rec_E += n
             if half != 1:
                 self.rec_H += n
+
+    def run_capture(self, n, curls, detectors):
+        """n full steps from time_steps_passed capturing curl_H on object boxes
+        (reverse-time adjoint); time_steps_passed += n."""
+        if n <= 0:
+            return
+        self._launch(n, 0, capture=(detectors, curls))
+        self.grid.time_steps_passed += n
 
     def run(self, n):
         """n full steps from time_steps_passed, then time_steps_passed += n."""

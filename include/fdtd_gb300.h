@@ -186,6 +186,64 @@ int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t
  * sampling and DFT accumulation after each half step. */
 int fdtd_run(fdtd_plan *plan, const fdtd_run_args *args, fdtd_stream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Reverse-time adjoint (no counterpart in the reference, which has no
+ * gradients; it stands in for autograd through the reference's torch
+ * backend).  The time step is affine in the state (E, H, PML auxiliaries),
+ * so the adjoint state (lam_E, lam_H and two adjoint auxiliaries per PML
+ * slab) evolves backwards under the transposed step, independent of the
+ * forward fields.  The gradient of a loss with respect to an object's
+ * inverse permittivity needs the forward curl_H on the object's box at every
+ * step; fdtd_run_capture stores it while running forward steps (the caller
+ * recomputes segments from its own field checkpoints).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    int32_t detectors;     /* 1: sample detectors and accumulate DFTs as fdtd_run does;
+                              0: skip them (recomputing a segment) */
+    int32_t n_curl;        /* entries of `curl`: 0 or the plan's object count */
+    void *const *curl;     /* HOST array of DEVICE pointers: per object NULL, or
+                              [n_steps][box cells][3] curl_H(H) on the object's box taken
+                              before each E half step (plan element type) */
+} fdtd_capture_args;
+
+/* fdtd_run (full steps only) plus the captures above. */
+int fdtd_run_capture(fdtd_plan *plan, const fdtd_run_args *args, const fdtd_capture_args *cap,
+                     fdtd_stream_t stream);
+
+typedef struct {
+    int64_t n_steps;       /* reverse steps of this call: forward steps top-1 down to top-n_steps */
+    int32_t parity;        /* which buffer of every aux pair holds the current adjoint auxiliaries;
+                              the call leaves them in buffer parity ^ (n_steps & 1) */
+    int32_t n_objects;     /* entries of `curl` and `grad`: the plan's object count */
+    void *lam_E;           /* [nx][ny][nz][3] adjoint of E, plan element type */
+    void *lam_H;
+    void *aux_E[FDTD_MAX_BOUNDARIES][2]; /* per PML boundary (grid.boundaries index): two
+                                            buffers of psi_E's layout; NULL for periodic */
+    void *aux_H[FDTD_MAX_BOUNDARIES][2];
+    const void *seed_E;    /* [rows][n_probe_cells][3] dL/d(trace_E), or NULL */
+    const void *seed_H;    /* [rows][n_probe_cells][3] dL/d(trace_H), or NULL */
+    int64_t seed_row;      /* seed row of the first reverse step; one less per step */
+    const double *const *dft_grad; /* HOST array of n_dft DEVICE pointers (NULL entries allowed):
+                                      dL/d(acc) as [n_freq][box cells][3][re, im] */
+    const double *phase;   /* [n_steps][n_phase_columns][2] (cos, -sin) of the DFT at the
+                              forward step of reverse step s, row s */
+    const void *const *curl;   /* HOST array: per object NULL or the captures of
+                                  fdtd_run_capture */
+    int64_t curl_row;      /* capture row of the first reverse step; one less per step */
+    double *const *grad;   /* HOST array: per object NULL or the gradient accumulator,
+                              [box cells][3] (FDTD_ITEM_OBJECT: dL/d inverse_permittivity) or
+                              [box cells][3][3] (FDTD_ITEM_ANISOTROPIC), added to */
+} fdtd_adjoint_args;
+
+/* n_steps reverse steps of the adjoint (float32 and float64 plans): per step
+ * the transposed H half then the transposed E half, with detector seeds added
+ * where the forward step sampled, hard-source cells zeroed, periodic copies
+ * transposed (lam[src] += lam[dst]; lam[dst] = 0), and gradient accumulation
+ * grad += courant * curl_H * lam_E on every object box with a grad pointer.
+ * Objects with a grad pointer must be FDTD_ITEM_OBJECT or
+ * FDTD_ITEM_ANISOTROPIC. */
+int fdtd_adjoint_run(fdtd_plan *plan, const fdtd_adjoint_args *args, fdtd_stream_t stream);
+
 /* curl_E (fdtd/grid.py:29-51) and curl_H (fdtd/grid.py:54-76) as
  * stand-alone kernels: out = curl(in), both [nx][ny][nz][3]. */
 int fdtd_curl_E(int32_t precision, const void *E, void *out, int32_t nx, int32_t ny, int32_t nz,
@@ -230,7 +288,7 @@ int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8);
 const char *fdtd_status_string(int32_t status);
 int32_t fdtd_last_cuda_error(void);
 /* sizeof of the ABI structs, for binding checks: 0 grid_desc, 1 boundary_desc,
- * 2 item_desc, 3 dft_desc, 4 run_args. */
+ * 2 item_desc, 3 dft_desc, 4 run_args, 5 capture_args, 6 adjoint_args. */
 size_t fdtd_abi_sizeof(int32_t which);
 
 #ifdef __cplusplus

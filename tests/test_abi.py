@@ -43,7 +43,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_struct_sizes_match(lib):
     for i, s in enumerate([_native.GridDesc, _native.BoundaryDesc, _native.ItemDesc, _native.DftDesc,
-                           _native.RunArgs]):
+                           _native.RunArgs, _native.CaptureArgs, _native.AdjointArgs]):
         assert lib.fdtd_abi_sizeof(i) == ctypes.sizeof(s), s.__name__
 
 
