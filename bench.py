@@ -13,7 +13,8 @@ the float64 and compensated float32 runs of the same grid, the float32 /
 float64 detector-trace error, the roofline of the fused half-step kernels
 (HBM-bound), the CPU oracle on a crop of the same generator, the end-to-end
 figure through the public API with per-step host<->device copies, launch
-count and SM clocks sampled during the timed region.
+count and SM clocks sampled during the timed region, and the cost of a
+differentiable run (adjoint) over a forward run on configs 4 and 5.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -59,8 +60,10 @@ def parse():
     p.add_argument("--variant", type=int, default=0, help="0 auto, 1 register streaming, 2 TMA-staged")
     p.add_argument("--tile-rows", type=int, default=0)
     p.add_argument("--stages", type=int, default=0)
+    p.add_argument("--pml-mode", type=int, default=0, help="0 auto, 1 PML inside the fused pass, 2 slab kernels")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--skip-adjoint", action="store_true", help="skip the adjoint/forward timing (configs 4, 5)")
     p.add_argument("--only", choices=["float32", "float32c", "float64"], default=None)
     return p.parse_args()
 
@@ -194,7 +197,8 @@ def build_grid(fd, scenes, prec, n, eps, args):
     pml = max(2, int(round(20 * n / 768))) if args.pml < 0 else args.pml
     g = scenes.c3(fd, n=n, pml=pml, eps=eps, detector=True)
     eng = g._ensure_engine()
-    eng.set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages, x_chunk=args.x_chunk)
+    eng.set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages, x_chunk=args.x_chunk,
+                   pml_mode=args.pml_mode)
     return g, eng
 
 
@@ -302,6 +306,66 @@ def cpu_oracle_rate(budget_s, n_full):
                       f"{dt:.1f} s, one host core (numpy elementwise is single-threaded)"}
 
 
+def adjoint_ratio(fd, scenes, which):
+    """Wall time of a differentiable run (fdtd_gb300.adjoint.run plus the
+    backward pass) over the wall time of the same forward run (grid.run),
+    configs 4 and 5 at full size, float32 fields and float64 gradients."""
+    import torch
+
+    def sync():
+        torch.cuda.synchronize()
+
+    out = {}
+    for cfg in which:
+        fd.set_backend("gb300.float32")
+        if cfg == "c4":
+            steps, K = 1000, 50
+            make = lambda: scenes.c4(fd)
+            design = lambda: torch.tensor(scenes.c4_design(48), device="cuda", requires_grad=True)
+            loss_of = lambda o: (o["detector"]["E"][800:, :, :, 0, 2].double() ** 2).sum()
+            desc = ("128^3, 12-cell PML, 48^3 design Object, plane source z=16, loss sum Ez^2 on the plane "
+                    "z=110 over steps 800-999")
+        else:
+            steps, K = 2000, 100
+            make = lambda: scenes.c5(fd)
+            design = lambda: torch.tensor(scenes.c5_tensors(96, 96, 48), device="cuda", requires_grad=True)
+            loss_of = lambda o: (o["dft"]["dft"][..., 0:2].abs() ** 2).sum()
+            desc = ("384x384x192, 20-cell PML, 96x96x48 anisotropic design (3x3 per cell), Gaussian plane "
+                    "source, loss sum over 1500/1550/1600 nm and the DFT plane of |F(Ex)|^2+|F(Ey)|^2")
+        g = make()
+        g.run(3, progress_bar=False)
+        sync()
+        t = time.perf_counter()
+        g.run(steps, progress_bar=False)
+        sync()
+        t_fwd = time.perf_counter() - t
+        del g
+        # warm-up differentiable run (loads the adjoint kernels), then the timed one
+        g = make()
+        p = design()
+        loss_of(fd.adjoint.run(g, 2 * K, {g.design: p}, checkpoint_every=K)).backward()
+        del g, p
+        gc.collect()
+        torch.cuda.empty_cache()
+        g = make()
+        p = design()
+        sync()
+        t = time.perf_counter()
+        outs = fd.adjoint.run(g, steps, {g.design: p}, checkpoint_every=K)
+        loss = loss_of(outs)
+        loss.backward()
+        sync()
+        t_adj = time.perf_counter() - t
+        out[cfg] = {"workload": desc, "steps": steps, "checkpoint_every": K, "forward_ms": t_fwd * 1e3,
+                    "adjoint_ms": t_adj * 1e3, "adjoint_over_forward": t_adj / t_fwd,
+                    "precision": "f32 fields, f64 gradient accumulation",
+                    "loss": float(loss.detach()), "grad_norm": float(p.grad.norm())}
+        del g, p, outs, loss
+        gc.collect()
+        torch.cuda.empty_cache()
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -383,6 +447,8 @@ def gb300_arm(args):
     if "float32c" in res:
         line["fp32c"] = {"value": res["float32c"]["gcells"], "ms_per_step": res["float32c"]["ms_per_step"]}
     line["nonfinite"] = {p: r["stats"]["nonfinite"] for p, r in res.items()}
+    if dist.rank == 0 and not args.skip_adjoint:
+        line["adjoint"] = adjoint_ratio(fd, scenes, ["c4", "c5"])
     if dist.rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_oracle_rate(args.cpu_seconds, n)
     if dist.rank == 0:

@@ -62,7 +62,7 @@ class GridDesc(ctypes.Structure):
     _fields_ = [
         ("abi_version", c_int32), ("precision", c_int32),
         ("nx", c_int32), ("ny", c_int32), ("nz", c_int32), ("x_chunk", c_int32),
-        ("variant", c_int32), ("tile_rows", c_int32), ("stages", c_int32), ("reserved", c_int32),
+        ("variant", c_int32), ("tile_rows", c_int32), ("stages", c_int32), ("pml_mode", c_int32),
         ("courant", ctypes.c_double),
         ("E", c_void_p), ("H", c_void_p), ("E_lo", c_void_p), ("H_lo", c_void_p),
         ("inv_eps", c_void_p), ("inv_mu", c_void_p),

@@ -202,12 +202,38 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                aligned16(d->inv_mu) && (!comp || (aligned16(d->E_lo) && aligned16(d->H_lo)));
     if (d->variant < 0 || d->variant > 2) return FDTD_ERR_ARGUMENT;
     if (d->variant == 2 && !vec) return FDTD_ERR_UNSUPPORTED;
+    if (d->pml_mode < 0 || d->pml_mode > 2) return FDTD_ERR_ARGUMENT;
+    // PML slabs in kernels of their own let the fused pass run without slab
+    // work (the staged kernels reach the HBM roofline there); the slab kernels
+    // re-read only the slab cells.  The per-cell order of the reference is
+    // kept: bulk and objects in the fused pass, then every boundary in
+    // registration order, then the sources.
+    p.pml_split = g.nslab > 0 &&
+                  (d->pml_mode == 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768));
+    if (p.pml_split) {
+        p.epi_E.clear();
+        for (int b = 0, s = 0; b < d->n_boundaries; ++b) {
+            const fdtd_boundary_desc &bd = d->boundaries[b];
+            EpiOp op{};
+            if (bd.kind == FDTD_BOUNDARY_PERIODIC) {
+                if (n[bd.axis] <= 1) continue;
+                op.kind = EPI_COPY;
+                op.axis = bd.axis;
+            } else {
+                op.kind = EPI_PML;
+                op.slab = s++;
+            }
+            p.epi_E.push_back(op);
+        }
+        p.epi_H = p.epi_E;
+    }
+    const int ks = p.pml_split ? 0 : g.nslab;  // slabs the fused pass handles
     // automatic choice: the TMA-staged kernels reach the HBM roofline on grids
     // without PML; with PML slabs the warps holding slab cells do more work per
     // plane and the staged kernels' per-plane CTA barrier makes the whole tile
     // wait for them, so the register-streaming kernels are faster there
     const bool tma = d->variant == 2 ||
-                     (d->variant == 0 && vec && g.nslab == 0 && (long)d->nz * 3 * (long)esize >= 768);
+                     (d->variant == 0 && vec && ks == 0 && (long)d->nz * 3 * (long)esize >= 768);
     Tiling t{};
     int ctas_per_sm = 2;
     bool use_tma = tma;
@@ -228,7 +254,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         };
         std::vector<Slot> slots;
         int slot_of[kMaxSlabs] = {0};
-        for (int s = 0; s < g.nslab; ++s) {
+        for (int s = 0; s < ks; ++s) {
             const SlabK &S = g.slab[s];
             const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? t.TY : Zc);
             const std::pair<int, int> rg(S.start / unit, (S.start + S.th - 1) / unit);
@@ -256,10 +282,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             sl.off = stage;
             stage += (sl.bytes + 127) & ~(size_t)127;
         }
-        for (int s = 0; s < g.nslab; ++s) g.psi_off[s] = (int)slots[slot_of[s]].off;
+        for (int s = 0; s < ks; ++s) g.psi_off[s] = (int)slots[slot_of[s]].off;
         g.stage_bytes = (int)stage;
         int coef = 0;
-        for (int s = 0; s < g.nslab; ++s) {
+        for (int s = 0; s < ks; ++s) {
             g.coef_off[s] = coef;
             coef += 2 * g.slab[s].th;
         }
@@ -378,8 +404,20 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     // sources inside the fused pass unless a periodic copy must come first
     const std::vector<ItemK> &cit = items;
+    auto touches_slab = [&](const ItemK &it) {
+        for (int s = 0; s < g.nslab; ++s) {
+            const SlabK &S = g.slab[s];
+            if (it.lo[S.axis] < S.start + S.th && it.hi[S.axis] > S.start) return true;
+        }
+        return false;
+    };
     auto can_fuse = [&](int first, int count) {
         if (p.epi_E.empty()) return true;
+        if (p.pml_split) {
+            for (int q = first; q < first + count; ++q)
+                if (touches_periodic_plane(cit[q], periodic_axes, n) || touches_slab(cit[q])) return false;
+            return true;
+        }
         if (slab_after_periodic) return false;
         for (int q = first; q < first + count; ++q)
             if (touches_periodic_plane(cit[q], periodic_axes, n)) return false;
@@ -494,6 +532,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                        : d->precision == FDTD_FLOAT32C ? prepare_tma_f32c(p)
                                                        : prepare_tma_f64(p);
         if (rc != FDTD_OK) return rc;
+    }
+
+    p.kf = p.k;
+    if (p.pml_split) {
+        p.kf.nslab = 0;
+        p.kf.nslab_fused = 0;
     }
 
     p.stats_ctas = 152 * 4;
@@ -707,7 +751,7 @@ int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8) {
     out8[3] = p.k.XC;
     out8[4] = (int64_t)p.grid.x * p.grid.y * p.grid.z;
     out8[5] = p.launches_per_step;
-    out8[6] = p.variant;
+    out8[6] = p.variant + (p.pml_split ? 10 : 0);
     out8[7] = p.k.stages;
     return FDTD_OK;
 }

@@ -231,6 +231,68 @@ __global__ void k_slab_correct(const GridK g, int s) {
     }
 }
 
+// One PML slab on its own (slabs outside the fused pass): the auxiliary
+// update of fdtd/boundaries.py:433-487 with the slab-local index rules, then
+// the correction of fdtd/boundaries.py:409-431, per slab cell and with the
+// same per-cell arithmetic as the fused pass.  The neighbour field is not
+// written during the half step, so its differences can be read here.
+template <class P, bool IS_E>
+__global__ void __launch_bounds__(kThreads) k_pml_slab(const GridK g, int s) {
+    using T = typename P::T;
+    const SlabK &S = g.slab[s];
+    const int a = S.axis;
+    const int n0 = a == 0 ? S.th : g.nx, n1 = a == 1 ? S.th : g.ny, n2 = a == 2 ? S.th : g.nz;
+    const int p2 = a == 2 ? S.thp : g.nz;
+    const long total = (long)n0 * n1 * n2;
+    const T c = courant_of<T>(g);
+    T *F = (T *)(IS_E ? g.E : g.H);
+    T *Flo = (T *)(IS_E ? g.Elo : g.Hlo);
+    const T *__restrict__ N = (const T *)(IS_E ? g.H : g.E);  // neighbour field
+    const T *__restrict__ M = (const T *)(IS_E ? g.ie : g.imu);
+    T *psi = (T *)(IS_E ? S.psiE : S.psiH);
+    const T *__restrict__ bt = (const T *)(IS_E ? S.bE : S.bH);
+    const T *__restrict__ ct = (const T *)(IS_E ? S.cE : S.cH);
+    const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+    const long stride = a == 0 ? 3L * g.ny * g.nz : (a == 1 ? 3L * g.nz : 3L);
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i0 = (int)(t / ((long)n1 * n2)), i1 = (int)((t / n2) % n1), i2 = (int)(t % n2);
+        const int l = a == 0 ? i0 : (a == 1 ? i1 : i2);
+        const int gi = a == 0 ? i0 + S.start : i0, gj = a == 1 ? i1 + S.start : i1, gk = a == 2 ? i2 + S.start : i2;
+        const size_t at = 3 * (((size_t)gi * g.ny + gj) * g.nz + gk);
+        const size_t pt = 2 * (((size_t)i0 * n1 + i1) * p2 + i2);
+        T p0 = psi[pt], p1 = psi[pt + 1];
+        const T b = bt[l], cc = ct[l];
+        if (IS_E ? (l >= 1) : (l <= S.th - 2)) {
+            // E: backward difference of H along the normal; H: forward difference of E
+            const T d0 = IS_E ? N[at + t2] - N[at - stride + t2] : N[at + stride + t2] - N[at + t2];
+            const T d1 = IS_E ? N[at + t1] - N[at - stride + t1] : N[at + stride + t1] - N[at + t1];
+            p0 = P::psi(p0, b, d0, cc);
+            p1 = P::psi(p1, b, d1, cc);
+        } else {
+            p0 = P::mul(p0, b);
+            p1 = P::mul(p1, b);
+        }
+        psi[pt] = p0;
+        psi[pt + 1] = p1;
+        T x1 = F[at + t1], x2 = F[at + t2];
+        T l1 = T(0), l2 = T(0);
+        if constexpr (P::COMP) {
+            l1 = Flo[at + t1];
+            l2 = Flo[at + t2];
+        }
+        pml_correct<P, IS_E>(x1, l1, P::mul(c, M[at + t1]), -p0);
+        pml_correct<P, IS_E>(x2, l2, P::mul(c, M[at + t2]), p1);
+        P::finish(x1, l1);
+        P::finish(x2, l2);
+        F[at + t1] = x1;
+        F[at + t2] = x2;
+        if constexpr (P::COMP) {
+            Flo[at + t1] = l1;
+            Flo[at + t2] = l2;
+        }
+    }
+}
+
 // Soft source points applied on their own: one thread per run of items that
 // share a cell, applied in order (a LineSource may list a cell twice).
 template <class P>

@@ -26,26 +26,26 @@ static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) 
     const CUtensorMap *m = p.maps;
     if (is_E)
         k_update_E_tma<P, TY><<<p.grid, block, p.smem_bytes, st>>>(
-            p.k, wave, m[MAP_H_NBR], m[MAP_E_OWN], m[MAP_IE], m[P::COMP ? MAP_ELO : MAP_E_OWN]);
+            p.kf, wave, m[MAP_H_NBR], m[MAP_E_OWN], m[MAP_IE], m[P::COMP ? MAP_ELO : MAP_E_OWN]);
     else
         k_update_H_tma<P, TY><<<p.grid, block, p.smem_bytes, st>>>(
-            p.k, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
+            p.kf, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
 }
 
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
     if (p.variant == 2) {
-        if (p.k.TY == 8) launch_tma<P, 8>(p, is_E, wave, st);
+        if (p.kf.TY == 8) launch_tma<P, 8>(p, is_E, wave, st);
         else launch_tma<P, 4>(p, is_E, wave, st);
         return;
     }
     if (p.V == 1) {
-        if (is_E) k_update_E<P, 1><<<p.grid, p.block, 0, st>>>(p.k, wave);
-        else k_update_H<P, 1><<<p.grid, p.block, 0, st>>>(p.k, wave);
+        if (is_E) k_update_E<P, 1><<<p.grid, p.block, 0, st>>>(p.kf, wave);
+        else k_update_H<P, 1><<<p.grid, p.block, 0, st>>>(p.kf, wave);
     } else {
-        if (is_E) k_update_E<P, VV><<<p.grid, p.block, 0, st>>>(p.k, wave);
-        else k_update_H<P, VV><<<p.grid, p.block, 0, st>>>(p.k, wave);
+        if (is_E) k_update_E<P, VV><<<p.grid, p.block, 0, st>>>(p.kf, wave);
+        else k_update_H<P, VV><<<p.grid, p.block, 0, st>>>(p.kf, wave);
     }
 }
 
@@ -72,6 +72,14 @@ static void launch_epilogue(Plan &p, bool is_E, const double *wave, cudaStream_t
                                    (S.axis == 2 ? S.th : g.nz);
                 if (is_E) k_slab_correct<P, true><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, op.slab);
                 else k_slab_correct<P, false><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, op.slab);
+                break;
+            }
+            case EPI_PML: {
+                const SlabK &S = g.slab[op.slab];
+                const long cells = (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) *
+                                   (S.axis == 2 ? S.th : g.nz);
+                if (is_E) k_pml_slab<P, true><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, op.slab);
+                else k_pml_slab<P, false><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, op.slab);
                 break;
             }
             case EPI_SOFT: {

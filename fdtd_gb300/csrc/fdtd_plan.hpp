@@ -11,12 +11,12 @@
 
 namespace fdtd {
 
-enum EpiKind { EPI_COPY = 0, EPI_SLAB = 1, EPI_SOFT = 2, EPI_HARD = 3 };
+enum EpiKind { EPI_COPY = 0, EPI_SLAB = 1, EPI_SOFT = 2, EPI_HARD = 3, EPI_PML = 4 };
 
 struct EpiOp {
     int kind;
     int axis;       // EPI_COPY
-    int slab;       // EPI_SLAB
+    int slab;       // EPI_SLAB (correction only), EPI_PML (auxiliary update and correction)
     int item;       // EPI_HARD
     int run_begin;  // EPI_SOFT
     int run_count;
@@ -27,7 +27,9 @@ enum MapId { MAP_H_NBR = 0, MAP_E_NBR, MAP_E_OWN, MAP_H_OWN, MAP_IE, MAP_MU, MAP
 
 struct Plan {
     int precision;
-    GridK k;
+    GridK k;           // the grid with every PML slab (epilogue and adjoint kernels)
+    GridK kf;          // what the fused pass sees: k, or k without slabs when they run on their own
+    int pml_split;     // 1: PML slabs run as EPI_PML kernels after the fused pass
     int V;             // cells per thread along z
     dim3 grid, block;  // fused-pass launch shape
     int variant;       // 1 register streaming, 2 TMA-staged

@@ -69,7 +69,7 @@ class Engine:
         self.grid = grid
         self.x_chunk = x_chunk
         # fused-pass kernel choice: variant 0 auto / 1 register streaming / 2 TMA-staged
-        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0}
+        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0}
         self.plan = None
         self._key = None
         self._keep = []
@@ -104,10 +104,12 @@ class Engine:
         self.x_chunk = int(x_chunk)
         self.refresh()
 
-    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None):
+    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None):
         """Choose the fused-pass kernels (0 auto, 1 register streaming, 2 TMA-staged),
-        the TMA tile rows (4 or 8) and ring stages; 0 keeps the automatic choice."""
-        for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages)):
+        the TMA tile rows (4 or 8) and ring stages, and where the PML slabs run
+        (0 auto, 1 inside the fused pass, 2 kernels of their own); 0 keeps the
+        automatic choice."""
+        for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode)):
             if v is not None:
                 self.tuning[k] = int(v)
         if x_chunk is not None:
@@ -120,7 +122,10 @@ class Engine:
         _native.check(_native.load().fdtd_plan_tiling(self.plan, out), "fdtd_plan_tiling")
         keys = ("cells_per_thread_z", "threads_z", "rows_y", "planes_x", "ctas", "launches_per_step",
                 "variant", "stages")
-        return dict(zip(keys, (int(v) for v in out)))
+        info = dict(zip(keys, (int(v) for v in out)))
+        info["pml_split"] = info["variant"] // 10
+        info["variant"] %= 10
+        return info
 
     def check_status(self):
         """Raise RuntimeError if a staged kernel reported a pipeline failure."""
@@ -172,6 +177,7 @@ class Engine:
         d.variant = self.tuning["variant"]
         d.tile_rows = self.tuning["tile_rows"]
         d.stages = self.tuning["stages"]
+        d.pml_mode = self.tuning["pml_mode"]
         d.courant = g.courant_number
         d.E, d.H = g._E.data_ptr(), g._H.data_ptr()
         d.E_lo = g._E_lo.data_ptr() if g._E_lo is not None else None

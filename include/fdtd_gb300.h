@@ -127,7 +127,8 @@ typedef struct {
                              2 TMA-staged (needs nz a multiple of 4 floats / 2 doubles) */
     int32_t tile_rows;    /* TMA-staged: rows per CTA, 4 or 8; 0 = automatic */
     int32_t stages;       /* TMA-staged: shared-memory ring depth, >= 2; 0 = automatic */
-    int32_t reserved;
+    int32_t pml_mode;     /* PML slabs: 0 automatic, 1 inside the fused pass, 2 one kernel per
+                             slab after the fused pass (auxiliary update and correction) */
     double courant;
     void *E;              /* [nx][ny][nz][3] */
     void *H;
@@ -282,7 +283,8 @@ int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_row
 
 /* Launch tiling chosen by the plan: out[0..7] = cells per thread along z,
  * threads along z, rows along y, planes along x per CTA, CTAs, kernels per
- * full step, variant (1 register streaming, 2 TMA-staged), ring stages. */
+ * full step, variant (1 register streaming, 2 TMA-staged; plus 10 when the
+ * PML slabs run in kernels of their own), ring stages. */
 int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8);
 
 const char *fdtd_status_string(int32_t status);
