@@ -322,7 +322,9 @@ def adjoint_ratio(fd, scenes, which):
             steps, K = 1000, 50
             make = lambda: scenes.c4(fd)
             design = lambda: torch.tensor(scenes.c4_design(48), device="cuda", requires_grad=True)
-            loss_of = lambda o: (o["detector"]["E"][800:, :, :, 0, 2].double() ** 2).sum()
+            # the last 200 records (steps 800-999 of the timed run); the warm-up run
+            # uses the same operations on its own last records
+            loss_of = lambda o: (o["detector"]["E"][-200:, :, :, 0, 2].double() ** 2).sum()
             desc = ("128^3, 12-cell PML, 48^3 design Object, plane source z=16, loss sum Ez^2 on the plane "
                     "z=110 over steps 800-999")
         else:

@@ -207,9 +207,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // work (the staged kernels reach the HBM roofline there); the slab kernels
     // re-read only the slab cells.  The per-cell order of the reference is
     // kept: bulk and objects in the fused pass, then every boundary in
-    // registration order, then the sources.
+    // registration order, then the sources.  Automatic choice: on grids below
+    // 8M cells a step takes tens of microseconds and the extra launches per
+    // slab cost more than the divergence they remove.
+    const long ncell = (long)d->nx * d->ny * d->nz;
     p.pml_split = g.nslab > 0 &&
-                  (d->pml_mode == 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768));
+                  (d->pml_mode == 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768 &&
+                                        ncell >= (8L << 20)));
     if (p.pml_split) {
         p.epi_E.clear();
         for (int b = 0, s = 0; b < d->n_boundaries; ++b) {
