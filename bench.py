@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-adjoint", action="store_true", help="skip the adjoint/forward timing (configs 4, 5)")
+    p.add_argument("--adjoint-only", choices=["c4", "c5", "both"], default=None,
+                   help="only the adjoint/forward timing of the named configs (prints its own JSON line)")
     p.add_argument("--only", choices=["float32", "float32c", "float64"], default=None)
     return p.parse_args()
 
@@ -513,6 +515,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.adjoint_only:
+        import fdtd_gb300 as fd
+        from fdtd_gb300 import scenes
+
+        which = ["c4", "c5"] if args.adjoint_only == "both" else [args.adjoint_only]
+        print(json.dumps({"adjoint": adjoint_ratio(fd, scenes, which)}), flush=True)
     else:
         gb300_arm(args)
 

@@ -662,6 +662,40 @@ int fdtd_curl_H(int32_t precision, const void *H, void *out, int32_t nx, int32_t
     return curl_common(precision, H, out, nx, ny, nz, stream, false);
 }
 
+}  // extern "C"
+
+namespace fdtd {
+// First pass of the field statistics into `rows` partial rows: 16-byte
+// vector loads for float fields whose value count is a multiple of 4.
+static void launch_stats_partial(const Plan &p, int rows, double *part, cudaStream_t st) {
+    const GridK &g = p.k;
+    const long nvals = 3L * g.nx * g.ny * g.nz;
+    const bool comp = p.precision == FDTD_FLOAT32C;
+    const bool vec = p.precision != FDTD_FLOAT64 && nvals % 4 == 0 && aligned16(g.E) && aligned16(g.H) &&
+                     (!comp || (aligned16(g.Elo) && aligned16(g.Hlo)));
+    if (vec) {
+        if (comp)
+            k_stats_partial4<true><<<rows, kThreads, 0, st>>>((const float4 *)g.E, (const float4 *)g.Elo,
+                                                              (const float4 *)g.H, (const float4 *)g.Hlo, nvals / 4,
+                                                              part);
+        else
+            k_stats_partial4<false><<<rows, kThreads, 0, st>>>((const float4 *)g.E, nullptr, (const float4 *)g.H,
+                                                               nullptr, nvals / 4, part);
+    } else if (p.precision == FDTD_FLOAT64) {
+        k_stats_partial<double, false><<<rows, kThreads, 0, st>>>((const double *)g.E, nullptr,
+                                                                 (const double *)g.H, nullptr, nvals, part);
+    } else if (comp) {
+        k_stats_partial<float, true><<<rows, kThreads, 0, st>>>((const float *)g.E, (const float *)g.Elo,
+                                                               (const float *)g.H, (const float *)g.Hlo, nvals, part);
+    } else {
+        k_stats_partial<float, false><<<rows, kThreads, 0, st>>>((const float *)g.E, nullptr, (const float *)g.H,
+                                                                nullptr, nvals, part);
+    }
+}
+}  // namespace fdtd
+
+extern "C" {
+
 size_t fdtd_stats_scratch_bytes(const fdtd_plan *plan) {
     if (!plan) return 0;
     return sizeof(double) * 5 * (size_t)plan->p.stats_ctas;
@@ -670,19 +704,9 @@ size_t fdtd_stats_scratch_bytes(const fdtd_plan *plan) {
 int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_stream_t stream) {
     if (!plan || !stats || !scratch) return FDTD_ERR_ARGUMENT;
     const Plan &p = plan->p;
-    const GridK &g = p.k;
-    const long nvals = 3L * g.nx * g.ny * g.nz;
     cudaStream_t st = (cudaStream_t)stream;
     double *part = (double *)scratch;
-    if (p.precision == FDTD_FLOAT64)
-        k_stats_partial<double, false><<<p.stats_ctas, kThreads, 0, st>>>(
-            (const double *)g.E, nullptr, (const double *)g.H, nullptr, nvals, part);
-    else if (p.precision == FDTD_FLOAT32C)
-        k_stats_partial<float, true><<<p.stats_ctas, kThreads, 0, st>>>(
-            (const float *)g.E, (const float *)g.Elo, (const float *)g.H, (const float *)g.Hlo, nvals, part);
-    else
-        k_stats_partial<float, false><<<p.stats_ctas, kThreads, 0, st>>>((const float *)g.E, nullptr,
-                                                                         (const float *)g.H, nullptr, nvals, part);
+    launch_stats_partial(p, p.stats_ctas, part, st);
     k_stats_final<<<1, 32, 0, st>>>(part, p.stats_ctas, stats);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
@@ -729,18 +753,8 @@ int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_row
     double *part = nullptr;
     const int rc = stats_rows_address(&part);
     if (rc != FDTD_OK) return rc;
-    const GridK &g = p.k;
-    const long nvals = 3L * g.nx * g.ny * g.nz;
     cudaStream_t st = (cudaStream_t)stream;
-    if (p.precision == FDTD_FLOAT64)
-        k_stats_partial<double, false><<<rows, kThreads, 0, st>>>((const double *)g.E, nullptr,
-                                                                 (const double *)g.H, nullptr, nvals, part);
-    else if (p.precision == FDTD_FLOAT32C)
-        k_stats_partial<float, true><<<rows, kThreads, 0, st>>>((const float *)g.E, (const float *)g.Elo,
-                                                               (const float *)g.H, (const float *)g.Hlo, nvals, part);
-    else
-        k_stats_partial<float, false><<<rows, kThreads, 0, st>>>((const float *)g.E, nullptr, (const float *)g.H,
-                                                                nullptr, nvals, part);
+    launch_stats_partial(p, rows, part, st);
     k_stats_final<<<1, 32, 0, st>>>(part, rows, stats);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FDTD_OK : cuda_fail(e);

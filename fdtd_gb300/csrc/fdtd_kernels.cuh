@@ -466,6 +466,85 @@ __global__ void __launch_bounds__(kThreads) k_stats_partial(const T *__restrict_
     }
 }
 
+// Float fields, first pass: 16-byte loads, squares of each 4-vector summed in
+// float and added to a double per vector, maxima in float.
+__device__ __forceinline__ void stats_vec4(float4 v, double &s, float &m, unsigned &bad) {
+    float q = 0.0f;
+    const float x[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        if (isfinite(x[c])) {
+            q = fmaf(x[c], x[c], q);
+            m = fmaxf(m, fabsf(x[c]));
+        } else {
+            bad++;
+        }
+    }
+    s += (double)q;
+}
+
+template <bool COMP>
+__global__ void __launch_bounds__(kThreads) k_stats_partial4(const float4 *__restrict__ E,
+                                                             const float4 *__restrict__ Elo,
+                                                             const float4 *__restrict__ H,
+                                                             const float4 *__restrict__ Hlo, long nvec,
+                                                             double *partial) {
+    double se = 0.0, sh = 0.0;
+    float fme = 0.0f, fmh = 0.0f;
+    unsigned nbad = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nvec; t += (long)gridDim.x * blockDim.x) {
+        float4 e = E[t], h = H[t];
+        if constexpr (COMP) {
+            const float4 el = Elo[t], hl = Hlo[t];
+            e.x += el.x;
+            e.y += el.y;
+            e.z += el.z;
+            e.w += el.w;
+            h.x += hl.x;
+            h.y += hl.y;
+            h.z += hl.z;
+            h.w += hl.w;
+        }
+        stats_vec4(e, se, fme, nbad);
+        stats_vec4(h, sh, fmh, nbad);
+    }
+    double me = fme, mh = fmh, bad = (double)nbad;
+    __shared__ double red[5][kThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        se += __shfl_down_sync(FULL_MASK, se, off);
+        sh += __shfl_down_sync(FULL_MASK, sh, off);
+        me = fmax(me, __shfl_down_sync(FULL_MASK, me, off));
+        mh = fmax(mh, __shfl_down_sync(FULL_MASK, mh, off));
+        bad += __shfl_down_sync(FULL_MASK, bad, off);
+    }
+    if (lane == 0) {
+        red[0][w] = se;
+        red[1][w] = sh;
+        red[2][w] = me;
+        red[3][w] = mh;
+        red[4][w] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0;
+        for (int q = 0; q < kThreads / 32; ++q) {
+            a0 += red[0][q];
+            a1 += red[1][q];
+            a2 = fmax(a2, red[2][q]);
+            a3 = fmax(a3, red[3][q]);
+            a4 += red[4][q];
+        }
+        double *row = partial + 5 * blockIdx.x;
+        row[0] = a0;
+        row[1] = a1;
+        row[2] = a2;
+        row[3] = a3;
+        row[4] = a4;
+    }
+}
+
 // Second pass: one thread folds the CTA rows in order (deterministic).
 static __global__ void k_stats_final(const double *partial, int nrows, double *out) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
