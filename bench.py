@@ -14,7 +14,8 @@ float64 detector-trace error, the roofline of the fused half-step kernels
 (HBM-bound), the CPU oracle on a crop of the same generator, the end-to-end
 figure through the public API with per-step host<->device copies, launch
 count and SM clocks sampled during the timed region, and the cost of a
-differentiable run (adjoint) over a forward run on configs 4 and 5.
+differentiable run (adjoint) over a forward run on configs 4 and 5, with the
+config-4 gradient checked against central finite differences.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -308,7 +309,40 @@ def cpu_oracle_rate(budget_s, n_full):
                       f"{dt:.1f} s, one host core (numpy elementwise is single-threaded)"}
 
 
-def adjoint_ratio(fd, scenes, which):
+def c4_finite_differences(fd, scenes, grad, loss_of, voxels=16, h=1e-3, seed=4):
+    """Central differences of the config-4 loss at random design voxels with
+    the float64 forward, against the adjoint gradient: relative L2 over the
+    sampled voxels."""
+    import numpy as np
+    import torch
+
+    fd.set_backend("gb300.float64")
+    base = scenes.c4_design(48)
+    rng = np.random.default_rng(seed)
+    flat = rng.choice(base.size, size=voxels, replace=False)
+    fdg, adj = [], []
+    t = time.perf_counter()
+    for f in flat:
+        idx = np.unravel_index(f, base.shape)
+        vals = []
+        for sgn in (1.0, -1.0):
+            d = base.copy()
+            d[idx] += sgn * h
+            g = scenes.c4(fd)
+            g.design.inverse_permittivity = torch.as_tensor(d)[..., None].expand(48, 48, 48, 3)
+            g.run(1000, progress_bar=False)
+            vals.append(float(loss_of({"detector": {"E": g.detector.E.tensor()}})))
+            del g
+        fdg.append((vals[0] - vals[1]) / (2 * h))
+        adj.append(float(grad[idx]))
+    fdg, adj = np.array(fdg), np.array(adj)
+    fd.set_backend("gb300.float32")
+    return {"voxels": voxels, "step": h, "forward": "f64", "seconds": time.perf_counter() - t,
+            "rel_l2": float(np.linalg.norm(adj - fdg) / np.linalg.norm(fdg)),
+            "max_rel": float(np.max(np.abs(adj - fdg) / np.maximum(np.abs(fdg), 1e-300)))}
+
+
+def adjoint_ratio(fd, scenes, which, fd_check=True):
     """Wall time of a differentiable run (fdtd_gb300.adjoint.run plus the
     backward pass) over the wall time of the same forward run (grid.run),
     configs 4 and 5 at full size, float32 fields and float64 gradients."""
@@ -364,6 +398,8 @@ def adjoint_ratio(fd, scenes, which):
                     "adjoint_ms": t_adj * 1e3, "adjoint_over_forward": t_adj / t_fwd,
                     "precision": "f32 fields, f64 gradient accumulation",
                     "loss": float(loss.detach()), "grad_norm": float(p.grad.norm())}
+        if cfg == "c4" and fd_check:
+            out[cfg]["fd_check"] = c4_finite_differences(fd, scenes, p.grad.detach().cpu().numpy(), loss_of)
         del g, p, outs, loss
         gc.collect()
         torch.cuda.empty_cache()

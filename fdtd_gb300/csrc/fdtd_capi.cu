@@ -322,11 +322,17 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (d->x_chunk > 0) {
         t.XC = d->x_chunk;
     } else {
-        // split x only when the (z, y) columns do not give two waves of CTAs
+        // register kernels: split x only when the (z, y) columns do not give
+        // two waves of CTAs.  Staged kernels (one CTA per SM): about twenty
+        // waves, so the partly filled last wave costs little (measured on
+        // 768^3: 3.8 waves 58.7, 7.6 waves 61.4, 22.7 waves 63.1 Gcell/s), with
+        // at least 32 planes per chunk (a chunk refills the ring and re-reads
+        // one halo plane)
         const long cols = (long)t.gz * t.gy;
-        const long target = 2L * n_sm * ctas_per_sm;
+        const long target = (use_tma ? 20L : 2L) * n_sm * ctas_per_sm;
         long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
-        chunks = std::max(1L, std::min(chunks, (long)d->nx));
+        const long max_chunks = use_tma ? std::max(1L, (long)d->nx / 32) : (long)d->nx;
+        chunks = std::max(1L, std::min(chunks, max_chunks));
         t.XC = (int)((d->nx + chunks - 1) / chunks);
     }
     t.gx = (d->nx + t.XC - 1) / t.XC;
