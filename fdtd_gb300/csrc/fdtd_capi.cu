@@ -202,7 +202,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                aligned16(d->inv_mu) && (!comp || (aligned16(d->E_lo) && aligned16(d->H_lo)));
     if (d->variant < 0 || d->variant > 2) return FDTD_ERR_ARGUMENT;
     if (d->variant == 2 && !vec) return FDTD_ERR_UNSUPPORTED;
-    if (d->pml_mode < 0 || d->pml_mode > 2) return FDTD_ERR_ARGUMENT;
+    if (d->pml_mode < 0 || d->pml_mode > 3) return FDTD_ERR_ARGUMENT;
     // PML slabs in kernels of their own let the fused pass run without slab
     // work (the staged kernels reach the HBM roofline there); the slab kernels
     // re-read only the slab cells.  The per-cell order of the reference is
@@ -210,13 +210,32 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // registration order, then the sources.  Automatic choice: on grids below
     // 8M cells a step takes tens of microseconds and the extra launches per
     // slab cost more than the divergence they remove.
+    //
+    // Mode 3 keeps the slabs normal to x or y that lead the boundary list
+    // inside the fused pass (their extra work is the same for every warp of a
+    // CTA) and splits off the rest.  Measured slower than splitting every slab
+    // (config 3: 58.0 vs 63.2 Gcell/s, config 5: 25.5 vs 32.3): the staged
+    // auxiliary rows shrink the shared-memory ring from 6 to 4 stages and the
+    // in-pass slab path costs more than the slab kernels' re-reads, so the
+    // automatic choice splits every slab.
     const long ncell = (long)d->nx * d->ny * d->nz;
     p.pml_split = g.nslab > 0 &&
-                  (d->pml_mode == 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768 &&
+                  (d->pml_mode >= 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768 &&
                                         ncell >= (8L << 20)));
+    int kfs = 0;  // leading slabs kept in the fused pass when split
+    if (p.pml_split && d->pml_mode == 3) {
+        while (kfs < d->n_boundaries && d->boundaries[kfs].kind == FDTD_BOUNDARY_PML &&
+               d->boundaries[kfs].axis != 2)
+            ++kfs;
+        if (kfs == g.nslab) {  // nothing left to split off
+            p.pml_split = 0;
+            kfs = 0;
+        }
+    }
+    p.fused_slabs = kfs;
     if (p.pml_split) {
         p.epi_E.clear();
-        for (int b = 0, s = 0; b < d->n_boundaries; ++b) {
+        for (int b = kfs, s = kfs; b < d->n_boundaries; ++b) {
             const fdtd_boundary_desc &bd = d->boundaries[b];
             EpiOp op{};
             if (bd.kind == FDTD_BOUNDARY_PERIODIC) {
@@ -231,24 +250,42 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         }
         p.epi_H = p.epi_E;
     }
-    const int ks = p.pml_split ? 0 : g.nslab;  // slabs the fused pass handles
+    const int ks = p.pml_split ? kfs : g.nslab;  // slabs the fused pass handles
     // automatic choice: the TMA-staged kernels reach the HBM roofline on grids
     // without PML; with PML slabs the warps holding slab cells do more work per
     // plane and the staged kernels' per-plane CTA barrier makes the whole tile
     // wait for them, so the register-streaming kernels are faster there
+    bool fused_z = false;  // a z slab inside the fused pass (divergent warps)
+    for (int s = 0; s < ks; ++s) fused_z |= g.slab[s].axis == 2;
     const bool tma = d->variant == 2 ||
-                     (d->variant == 0 && vec && ks == 0 && (long)d->nz * 3 * (long)esize >= 768);
+                     (d->variant == 0 && vec && !fused_z && (long)d->nz * 3 * (long)esize >= 768);
     Tiling t{};
     int ctas_per_sm = 2;
     bool use_tma = tma;
     if (use_tma) {
         t.V = vmax;
-        t.TZ = 32;
-        if (d->tile_rows != 0 && d->tile_rows != 4 && d->tile_rows != 8) return FDTD_ERR_ARGUMENT;
-        t.TY = d->tile_rows ? d->tile_rows : 8;
+        if (d->tile_rows != 0 && d->tile_rows != 4 && d->tile_rows != 8 && d->tile_rows != 16)
+            return FDTD_ERR_ARGUMENT;
+        // tile shapes: 32 threads along z x 8 (or 4) rows, or 16 x 16.  The
+        // 16-wide tile fits z extents that are a multiple of 16 V but not of
+        // 32 V (config 5: nz = 192) and needs one halo row per 16 rows; its
+        // stage holds the auxiliary rows of at most 4 slabs (64 lanes' worth)
+        int rows = d->tile_rows;
+        if (rows == 0) {
+            const long z32 = 32L * vmax, z16 = 16L * vmax;
+            const long waste32 = (d->nz + z32 - 1) / z32 * z32 - d->nz;
+            const long waste16 = (d->nz + z16 - 1) / z16 * z16 - d->nz;
+            rows = (waste16 < waste32 && ks <= 4) ? 16 : 8;
+        }
+        if (rows == 16 && ks > 4) {
+            if (d->variant == 2 && d->tile_rows == 16) return FDTD_ERR_UNSUPPORTED;
+            rows = 8;
+        }
+        t.TY = rows;
+        t.TZ = rows == 16 ? 16 : 32;
         // stage layout: field tiles, then one PML auxiliary slot per group of
         // slabs of one axis that never meet in the same tile (rows copied per stage)
-        const int Zc = 32 * t.V;
+        const int Zc = t.TZ * t.V;
         const size_t field = tma_stage_bytes(d->precision, t.TY);
         struct Slot {
             int axis;
@@ -414,8 +451,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     // sources inside the fused pass unless a periodic copy must come first
     const std::vector<ItemK> &cit = items;
-    auto touches_slab = [&](const ItemK &it) {
-        for (int s = 0; s < g.nslab; ++s) {
+    auto touches_slab = [&](const ItemK &it) {  // a slab corrected after the fused pass
+        for (int s = p.fused_slabs; s < g.nslab; ++s) {
             const SlabK &S = g.slab[s];
             if (it.lo[S.axis] < S.start + S.th && it.hi[S.axis] > S.start) return true;
         }
@@ -546,8 +583,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     p.kf = p.k;
     if (p.pml_split) {
-        p.kf.nslab = 0;
-        p.kf.nslab_fused = 0;
+        p.kf.nslab = p.fused_slabs;
+        p.kf.nslab_fused = p.fused_slabs;
     }
 
     p.stats_ctas = 152 * 4;

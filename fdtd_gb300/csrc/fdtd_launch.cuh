@@ -20,24 +20,26 @@ static int check_launch() {
     return FDTD_OK;
 }
 
-template <class P, int TY>
+template <class P, int TZ, int TY>
 static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
-    const dim3 block(kTmaTZ, TY, 1);
+    const dim3 block(TZ, TY, 1);
     const CUtensorMap *m = p.maps;
     if (is_E)
-        k_update_E_tma<P, TY><<<p.grid, block, p.smem_bytes, st>>>(
+        k_update_E_tma<P, TZ, TY><<<p.grid, block, p.smem_bytes, st>>>(
             p.kf, wave, m[MAP_H_NBR], m[MAP_E_OWN], m[MAP_IE], m[P::COMP ? MAP_ELO : MAP_E_OWN]);
     else
-        k_update_H_tma<P, TY><<<p.grid, block, p.smem_bytes, st>>>(
+        k_update_H_tma<P, TZ, TY><<<p.grid, block, p.smem_bytes, st>>>(
             p.kf, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
 }
 
+// Staged-kernel tile shapes (threads along z x rows): 32x8, 32x4, 16x16.
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
     if (p.variant == 2) {
-        if (p.kf.TY == 8) launch_tma<P, 8>(p, is_E, wave, st);
-        else launch_tma<P, 4>(p, is_E, wave, st);
+        if (p.kf.TY == 16) launch_tma<P, 16, 16>(p, is_E, wave, st);
+        else if (p.kf.TY == 8) launch_tma<P, 32, 8>(p, is_E, wave, st);
+        else launch_tma<P, 32, 4>(p, is_E, wave, st);
         return;
     }
     if (p.V == 1) {
@@ -125,9 +127,9 @@ static bool encode_field_map(CUtensorMap *m, const void *base, const GridK &g, i
     return r == CUDA_SUCCESS;
 }
 
-template <class P, int TY>
+template <class P, int TZ, int TY>
 static int prepare_tma_rows(Plan &p) {
-    using G = StageGeom<typename P::T, TY, P::COMP>;
+    using G = StageGeom<typename P::T, TZ, TY, P::COMP>;
     const GridK &g = p.k;
     const int es = (int)sizeof(typename P::T);
     bool ok = encode_field_map(&p.maps[MAP_H_NBR], g.H, g, es, G::boxN, TY + 1) &&
@@ -143,10 +145,10 @@ static int prepare_tma_rows(Plan &p) {
     p.k.field_tx = (int)G::txBytes;
     p.smem_bytes = (size_t)g.stages * g.stage_bytes + (size_t)g.stages * 8 +
                    (size_t)g.coef_values * sizeof(typename P::T) + 128;
-    cudaError_t e = cudaFuncSetAttribute(k_update_E_tma<P, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_update_E_tma<P, TZ, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)p.smem_bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_update_H_tma<P, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(k_update_H_tma<P, TZ, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)p.smem_bytes);
     if (e != cudaSuccess) {
         set_last_cuda_error((int)e);
@@ -157,13 +159,15 @@ static int prepare_tma_rows(Plan &p) {
 
 template <class P>
 static int prepare_tma_impl(Plan &p) {
-    return p.k.TY == 8 ? prepare_tma_rows<P, 8>(p) : prepare_tma_rows<P, 4>(p);
+    if (p.k.TY == 16) return prepare_tma_rows<P, 16, 16>(p);
+    return p.k.TY == 8 ? prepare_tma_rows<P, 32, 8>(p) : prepare_tma_rows<P, 32, 4>(p);
 }
 
 template <class P>
 static size_t stage_bytes_of(int tile_rows) {
-    return tile_rows == 8 ? (size_t)StageGeom<typename P::T, 8, P::COMP>::stageBytes
-                          : (size_t)StageGeom<typename P::T, 4, P::COMP>::stageBytes;
+    if (tile_rows == 16) return (size_t)StageGeom<typename P::T, 16, 16, P::COMP>::stageBytes;
+    return tile_rows == 8 ? (size_t)StageGeom<typename P::T, 32, 8, P::COMP>::stageBytes
+                          : (size_t)StageGeom<typename P::T, 32, 4, P::COMP>::stageBytes;
 }
 
 // n_steps full steps (or one half step).  With capture arguments: detectors

@@ -29,7 +29,8 @@ struct Plan {
     int precision;
     GridK k;           // the grid with every PML slab (epilogue and adjoint kernels)
     GridK kf;          // what the fused pass sees: k, or k without slabs when they run on their own
-    int pml_split;     // 1: PML slabs run as EPI_PML kernels after the fused pass
+    int pml_split;     // 1: PML slabs from fused_slabs on run as EPI_PML kernels after the fused pass
+    int fused_slabs;   // with pml_split: leading slabs (normal to x or y) kept in the fused pass
     int V;             // cells per thread along z
     dim3 grid, block;  // fused-pass launch shape
     int variant;       // 1 register streaming, 2 TMA-staged

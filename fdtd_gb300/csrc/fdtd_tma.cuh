@@ -27,7 +27,6 @@
 
 namespace fdtd {
 
-constexpr int kTmaTZ = 32;
 constexpr unsigned kWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -79,11 +78,12 @@ __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier
 
 // Byte layout of the field part of one stage: the neighbour tile (TY+1 rows
 // of 3*Zc+4 values) then the own tiles (TY rows of 3*Zc values each),
-// 128-byte aligned.  The PML auxiliary slots follow at g.psi_off[s].
-template <class T, int TY, bool COMP>
+// 128-byte aligned.  The PML auxiliary slots follow at g.psi_off[s].  A tile
+// is TZ threads (V cells each) along z by TY rows.
+template <class T, int TZ, int TY, bool COMP>
 struct StageGeom {
     static constexpr int V = sizeof(T) == 4 ? 4 : 2;
-    static constexpr int Zc = kTmaTZ * V;  // cells per tile row
+    static constexpr int Zc = TZ * V;  // cells per tile row
     static constexpr int pitchN = 3 * Zc + 4;  // values per neighbour row
     static constexpr int pitchO = 3 * Zc;
     static constexpr int nbrBytes = (TY + 1) * pitchN * (int)sizeof(T);
@@ -99,7 +99,7 @@ struct StageGeom {
     static constexpr int boxO = pitchO * (int)sizeof(T) / 8;
 };
 
-// Fill one stage for plane p (warp 0, all lanes).  The PML auxiliary rows of
+// Fill one stage for plane p (warp 0 of the CTA, all lanes).  The PML auxiliary rows of
 // every slab crossing the tile at plane p are copied with 1D bulk copies (one
 // row per lane), then lane 0 arms the stage barrier with the total byte count
 // and issues the field tiles.
@@ -108,7 +108,7 @@ __device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, ui
                                            bool is_E, int k0c, int j0, int Zc, const CUtensorMap *tmN, int xN,
                                            int yN, const CUtensorMap *tmF, const CUtensorMap *tmM,
                                            const CUtensorMap *tmL, bool comp, int xO, int ownOff, int ownStride) {
-    const int lane = threadIdx.x;
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
     uint32_t bytes[2] = {0u, 0u};
     const void *srcp[2] = {nullptr, nullptr};
     uint32_t dst[2] = {0u, 0u};
@@ -168,13 +168,13 @@ __device__ __forceinline__ void stage_coef_tables(const GridK &g, T *tab, bool i
     }
 }
 
-template <class P, int TY>
-__global__ void __launch_bounds__(kTmaTZ *TY)
+template <class P, int TZ, int TY>
+__global__ void __launch_bounds__(TZ *TY)
     k_update_E_tma(const GridK g, const double *__restrict__ wave, const __grid_constant__ CUtensorMap tmN,
                    const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmM,
                    const __grid_constant__ CUtensorMap tmL) {
     using T = typename P::T;
-    using G = StageGeom<T, TY, P::COMP>;
+    using G = StageGeom<T, TZ, TY, P::COMP>;
     constexpr int V = G::V;
     constexpr int N = 3 * V;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
     const int SB = g.stage_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)S * SB);
     T *ctab = reinterpret_cast<T *>(smem + (size_t)S * SB + 8 * (size_t)S);
-    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kTmaTZ + tz;
+    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
     };
     int issued = 0;
     for (; issued < min(S, np); ++issued)
-        if (ty == 0) issue(issued);
+        if (tid < 32) issue(issued);
 
     const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
     alignas(16) T hp[N];  // H at plane i-1 (registers)
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
         __syncthreads();
         if (abort_flag) break;
         if (issued < np) {
-            if (ty == 0) {
+            if (tid < 32) {
                 fence_proxy_async();
                 issue(issued);
             }
@@ -279,13 +279,13 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
     }
 }
 
-template <class P, int TY>
-__global__ void __launch_bounds__(kTmaTZ *TY)
+template <class P, int TZ, int TY>
+__global__ void __launch_bounds__(TZ *TY)
     k_update_H_tma(const GridK g, const double *__restrict__ wave, const __grid_constant__ CUtensorMap tmN,
                    const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmM,
                    const __grid_constant__ CUtensorMap tmL) {
     using T = typename P::T;
-    using G = StageGeom<T, TY, P::COMP>;
+    using G = StageGeom<T, TZ, TY, P::COMP>;
     constexpr int V = G::V;
     constexpr int N = 3 * V;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
     const int SB = g.stage_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)S * SB);
     T *ctab = reinterpret_cast<T *>(smem + (size_t)S * SB + 8 * (size_t)S);
-    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kTmaTZ + tz;
+    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
     };
     int issued = 0;
     for (; issued < min(S, nfill); ++issued)
-        if (ty == 0) issue(issued);
+        if (tid < 32) issue(issued);
 
     const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
     int r = 0;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(kTmaTZ *TY)
         __syncthreads();
         if (abort_flag) break;
         if (issued < nfill) {
-            if (ty == 0) {
+            if (tid < 32) {
                 fence_proxy_async();
                 issue(issued);
             }

@@ -106,7 +106,8 @@ class Engine:
 
     def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None):
         """Choose the fused-pass kernels (0 auto, 1 register streaming, 2 TMA-staged),
-        the TMA tile rows (4 or 8) and ring stages, and where the PML slabs run
+        the TMA tile rows (4 or 8 with 32-thread-wide tiles, 16 with 16-wide) and
+        ring stages, and where the PML slabs run
         (0 auto, 1 inside the fused pass, 2 kernels of their own); 0 keeps the
         automatic choice."""
         for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode)):

@@ -125,10 +125,13 @@ typedef struct {
     int32_t x_chunk;      /* planes per CTA along x; 0 = automatic */
     int32_t variant;      /* fused-pass kernels: 0 automatic, 1 register streaming,
                              2 TMA-staged (needs nz a multiple of 4 floats / 2 doubles) */
-    int32_t tile_rows;    /* TMA-staged: rows per CTA, 4 or 8; 0 = automatic */
+    int32_t tile_rows;    /* TMA-staged: rows per CTA, 4 or 8 (tiles 32 threads wide along z)
+                             or 16 (16 threads wide); 0 = automatic */
     int32_t stages;       /* TMA-staged: shared-memory ring depth, >= 2; 0 = automatic */
     int32_t pml_mode;     /* PML slabs: 0 automatic, 1 inside the fused pass, 2 one kernel per
-                             slab after the fused pass (auxiliary update and correction) */
+                             slab after the fused pass (auxiliary update and correction),
+                             3 the slabs normal to x or y that lead the boundary list inside
+                             the fused pass and the others in kernels of their own */
     double courant;
     void *E;              /* [nx][ny][nz][3] */
     void *H;

@@ -178,7 +178,11 @@ def test_run_step_and_halves_agree(fd):
 TILINGS = [dict(variant=1, x_chunk=1), dict(variant=1, x_chunk=7), dict(variant=2, tile_rows=8, stages=2),
            dict(variant=2, tile_rows=4, stages=3, x_chunk=5), dict(variant=2, tile_rows=8, stages=3, x_chunk=24),
            dict(variant=1, pml_mode=2), dict(variant=2, tile_rows=8, stages=2, pml_mode=2),
-           dict(variant=2, tile_rows=4, stages=3, x_chunk=5, pml_mode=2)]
+           dict(variant=2, tile_rows=4, stages=3, x_chunk=5, pml_mode=2),
+           dict(variant=2, tile_rows=16, stages=2, pml_mode=2), dict(variant=2, tile_rows=16, stages=3, x_chunk=6,
+                                                                 pml_mode=2),
+           dict(variant=2, tile_rows=8, stages=3, pml_mode=3), dict(variant=1, pml_mode=3, x_chunk=5),
+           dict(variant=2, tile_rows=16, stages=2, pml_mode=3)]
 
 
 @pytest.mark.parametrize("prec", ["float64", "float32", "float32c"])
@@ -198,21 +202,22 @@ def test_kernel_variants_and_tiling_agree_bitwise(fd, prec):
         g._ensure_engine().set_tuning(**tune)
         info = g._engine.tiling()
         assert info["variant"] == tune["variant"]
-        assert info["pml_split"] == (1 if tune.get("pml_mode") == 2 else 0)
+        assert info["pml_split"] == (1 if tune.get("pml_mode", 1) >= 2 else 0)
         g.run(20, progress_bar=False)
-        if prec == "float32c" and tune.get("pml_mode") == 2:
+        if prec == "float32c" and tune.get("pml_mode", 1) >= 2:
             assert rel_l2(g.E, ref.E) <= 1e-6 and rel_l2(g.H, ref.H) <= 1e-6, tune
             continue
         assert torch.equal(g.E, ref.E) and torch.equal(g.H, ref.H), tune
         assert np.array_equal(np.asarray(g.detector.E), np.asarray(ref.detector.E)), tune
 
 
-@pytest.mark.parametrize("pml_mode", [1, 2])
+@pytest.mark.parametrize("tile_rows", [8, 16])
+@pytest.mark.parametrize("pml_mode", [1, 2, 3])
 @pytest.mark.parametrize("prec", ["float64", "float32"])
-def test_tma_variant_on_wide_grid_against_oracle(fd, prec, pml_mode):
+def test_tma_variant_on_wide_grid_against_oracle(fd, prec, pml_mode, tile_rows):
     """A grid wider than one TMA tile along z and y (several CTAs, tile edges,
     periodic x, PML on y/z, objects crossing tile borders), PML slabs inside
-    the fused pass or in kernels of their own."""
+    the fused pass or in kernels of their own, 32x8 and 16x16 tiles."""
     fd.set_backend("gb300." + prec)
     from fdtd_gb300 import scenes
 
@@ -231,9 +236,9 @@ def test_tma_variant_on_wide_grid_against_oracle(fd, prec, pml_mode):
         return g
 
     g, o = build(fd), build(fo)
-    g._ensure_engine().set_tuning(variant=2, pml_mode=pml_mode)
-    assert g._engine.tiling()["variant"] == 2
-    assert g._engine.tiling()["pml_split"] == pml_mode - 1
+    g._ensure_engine().set_tuning(variant=2, pml_mode=pml_mode, tile_rows=tile_rows)
+    assert g._engine.tiling()["variant"] == 2 and g._engine.tiling()["rows_y"] == tile_rows
+    assert g._engine.tiling()["pml_split"] == (1 if pml_mode >= 2 else 0)
     g.run(40, progress_bar=False)
     o.run(40)
     tol = TOL64 if prec == "float64" else TOL32
