@@ -51,6 +51,13 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
     g.XC = p.adj_XC;
     T *LE = (T *)a->lam_E;
     T *LH = (T *)a->lam_H;
+    // plans that run the forward PML slabs in kernels of their own do the same
+    // for the transposes: slab-free bulk passes, then one kernel per slab
+    GridK gb = g;
+    if (p.pml_split) gb.nslab = 0;
+    auto slab_cells = [&](const SlabK &S) {
+        return (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) * (S.axis == 2 ? S.th : g.nz);
+    };
     const int pblocks = (3 * p.n_probe + kThreads - 1) / kThreads;
     int par = a->parity;
     for (int64_t s = 0; s < a->n_steps; ++s) {
@@ -86,7 +93,10 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
                     g, op.slab, (T *)a->aux_H[p.slab_boundary[op.slab]][par]);
             }
         }
-        k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(g, x);
+        k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
+        if (p.pml_split)
+            for (int q = 0; q < g.nslab; ++q)
+                k_adj_slab<T, false><<<grid_stride_blocks(slab_cells(g.slab[q])), kThreads, 0, st>>>(g, x, q);
 
         // transposed E half
         if (a->seed_E && p.n_probe)
@@ -118,7 +128,10 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
                     g, op.slab, (T *)a->aux_E[p.slab_boundary[op.slab]][par]);
             }
         }
-        k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(g, x);
+        k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
+        if (p.pml_split)
+            for (int q = 0; q < g.nslab; ++q)
+                k_adj_slab<T, true><<<grid_stride_blocks(slab_cells(g.slab[q])), kThreads, 0, st>>>(g, x, q);
         for (int q = p.n_objects - 1; q >= 0; --q) {
             const ItemK &o = p.items_host[q];
             const long reach = (long)(o.hi[0] - std::max(0, o.lo[0] - 1)) * (o.hi[1] - std::max(0, o.lo[1] - 1)) *

@@ -343,6 +343,77 @@ __global__ void __launch_bounds__(kThreads) k_adj_E(const GridK g, const AdjAux 
     }
 }
 
+// PML transposes of one slab on their own (plans whose forward pass runs the
+// slabs in kernels of their own): the per-cell terms of adj_slab_E (IS_E,
+// transposed E half: lam_H and the E-side adjoint auxiliaries, after k_adj_E)
+// or adj_slab_H (lam_E and the H-side ones, after k_adj_H).  The kernel reads
+// the adjoint field it does not write, and the current auxiliary buffer.
+template <class T, bool IS_E>
+__global__ void __launch_bounds__(kThreads) k_adj_slab(const GridK g, const AdjAux x, int s) {
+    const SlabK &S = g.slab[s];
+    const int a = S.axis, th = S.th;
+    const int n0 = a == 0 ? th : g.nx, n1 = a == 1 ? th : g.ny, n2 = a == 2 ? th : g.nz;
+    const long total = (long)n0 * n1 * n2;
+    const T c = courant_of<T>(g);
+    const T *L = (const T *)(IS_E ? g.E : g.H);  // lam_E (E half) or lam_H (H half), read
+    T *O = (T *)(IS_E ? g.H : g.E);              // the adjoint field updated
+    const T *__restrict__ M = (const T *)(IS_E ? g.ie : g.imu);
+    const T *ao = (const T *)(IS_E ? x.Eo[s] : x.Ho[s]);
+    T *an = (T *)(IS_E ? x.En[s] : x.Hn[s]);
+    const T *__restrict__ bt = (const T *)(IS_E ? S.bE : S.bH);
+    const T *__restrict__ ct = (const T *)(IS_E ? S.cE : S.cH);
+    const T f = s < g.nslab_fused ? T(1) : T(0);
+    const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+    // one step along the normal, in cells and in auxiliary pairs (same count)
+    const long cstride = a == 0 ? (long)g.ny * g.nz : (a == 1 ? (long)g.nz : 1L);
+    const long pstride = cstride;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i0 = (int)(t / ((long)n1 * n2)), i1 = (int)((t / n2) % n1), i2 = (int)(t % n2);
+        const int l = a == 0 ? i0 : (a == 1 ? i1 : i2);
+        const int gi = a == 0 ? i0 + S.start : i0, gj = a == 1 ? i1 + S.start : i1, gk = a == 2 ? i2 + S.start : i2;
+        const size_t cell = ((size_t)gi * g.ny + gj) * g.nz + gk;
+        const long pt = slab_pair(g, S, gi, gj, gk);
+        const T v1 = (c * M[3 * cell + t1]) * L[3 * cell + t1];
+        const T v2 = (c * M[3 * cell + t2]) * L[3 * cell + t2];
+        T d0 = T(0), d1 = T(0), a0, a1;
+        if (IS_E) {
+            a0 = ao[2 * pt] - f * v1;
+            a1 = ao[2 * pt + 1] + f * v2;
+            if (l >= 1) {
+                d0 = -(ct[l] * a0);
+                d1 = -(ct[l] * a1);
+            }
+            if (l <= th - 2) {
+                const size_t nc = cell + cstride;
+                const long pq = pt + pstride;
+                const T q0 = ao[2 * pq] - f * ((c * M[3 * nc + t1]) * L[3 * nc + t1]);
+                const T q1 = ao[2 * pq + 1] + f * ((c * M[3 * nc + t2]) * L[3 * nc + t2]);
+                d0 += ct[l + 1] * q0;
+                d1 += ct[l + 1] * q1;
+            }
+        } else {
+            a0 = ao[2 * pt] + f * v1;
+            a1 = ao[2 * pt + 1] - f * v2;
+            if (l <= th - 2) {
+                d0 = ct[l] * a0;
+                d1 = ct[l] * a1;
+            }
+            if (l >= 1) {
+                const size_t pc = cell - cstride;
+                const long pq = pt - pstride;
+                const T p0 = ao[2 * pq] + f * ((c * M[3 * pc + t1]) * L[3 * pc + t1]);
+                const T p1 = ao[2 * pq + 1] - f * ((c * M[3 * pc + t2]) * L[3 * pc + t2]);
+                d0 -= ct[l - 1] * p0;
+                d1 -= ct[l - 1] * p1;
+            }
+        }
+        O[3 * cell + t2] -= d0;
+        O[3 * cell + t1] -= d1;
+        an[2 * pt] = bt[l] * a0;
+        an[2 * pt + 1] = bt[l] * a1;
+    }
+}
+
 // u_obj = (d E_after / d curl_H)^T lam_E of one object at cell (i, j, k),
 // zero outside its box.  Object: coef0 = courant*inverse_permittivity;
 // absorbing: courant*inverse_permittivity/(1+f); anisotropic: courant*M^T.

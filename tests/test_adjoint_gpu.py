@@ -40,10 +40,12 @@ def native():
     return _native.load()
 
 
-def gb_loss_and_grad(fd, sc, design_values, precision, checkpoint_every):
+def gb_loss_and_grad(fd, sc, design_values, precision, checkpoint_every, pml_mode=0):
     fd.set_backend("gb300." + precision)
     grid, obj = sc.build(fd)
     sc.detectors(fd, grid)
+    if pml_mode:
+        grid._ensure_engine().set_tuning(pml_mode=pml_mode)
     p = torch.tensor(np.asarray(design_values), dtype=torch.float64, device="cuda", requires_grad=True)
     outs = fd.adjoint.run(grid, sc.steps, design={obj: p}, checkpoint_every=checkpoint_every)
     loss = sc.gb_loss(outs, torch)
@@ -61,6 +63,19 @@ def test_adjoint_matches_reference_autograd(fd, name, precision):
     assert abs(loss - float(ref["loss"])) <= tol * abs(float(ref["loss"]))
     err = rel_l2(grad, ref["grad"])
     assert err <= tol, f"{name} {precision}: gradient relative L2 {err:.3e}"
+
+
+@pytest.mark.parametrize("name", sorted(adjoint_scenes.SCENES))
+def test_adjoint_with_pml_slab_kernels_matches_reference_autograd(fd, name):
+    """Plans that run the PML slabs in kernels of their own (the choice on
+    large grids) run the PML transposes in kernels of their own too."""
+    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    sc = adjoint_scenes.SCENES[name]
+    loss, grad, grid = gb_loss_and_grad(fd, sc, ref["design"], "float64", checkpoint_every=9, pml_mode=2)
+    assert grid._engine.tiling()["pml_split"] == 1
+    assert abs(loss - float(ref["loss"])) <= TOL64 * abs(float(ref["loss"]))
+    err = rel_l2(grad, ref["grad"])
+    assert err <= TOL64, f"{name}: gradient relative L2 {err:.3e}"
 
 
 def test_checkpoint_interval_does_not_change_the_gradient(fd):
@@ -128,7 +143,8 @@ class MixedScene:
         return (e ** 2).sum() + 0.5 * (h[..., 1] * h[..., 2]).sum()
 
 
-def test_adjoint_matches_oracle_on_every_stage(fd):
+@pytest.mark.parametrize("pml_mode", [0, 2])
+def test_adjoint_matches_oracle_on_every_stage(fd, pml_mode):
     sc = MixedScene()
     design = sc.design()
     grid, obj = sc.build(fo)
@@ -140,7 +156,7 @@ def test_adjoint_matches_oracle_on_every_stage(fd):
     loss.backward()
     seeds = {n: {k: (None if t.grad is None else t.grad.numpy()) for k, t in r.items()} for n, r in outs.items()}
     want = fa.adjoint_gradient(grid, sc.steps, obj, 0, seeds, curls).sum(axis=-1)
-    got_loss, got, _ = gb_loss_and_grad(fd, sc, design, "float64", checkpoint_every=5)
+    got_loss, got, _ = gb_loss_and_grad(fd, sc, design, "float64", checkpoint_every=5, pml_mode=pml_mode)
     assert abs(got_loss - float(loss.detach())) <= 1e-10 * abs(float(loss.detach()))
     err = rel_l2(got, want)
     assert err <= TOL64, err
