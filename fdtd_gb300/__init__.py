@@ -21,6 +21,7 @@ __version__ = "0.1.0"
 from .backend import backend, set_backend
 from .boundaries import DomainBorderPML, PeriodicBoundary, PML
 from .detectors import BlockDetector, CurrentDetector, DFTPlaneDetector, LineDetector, PlaneDetector
+from .fourier import FrequencyRoutines
 from .grid import Grid
 from .objects import AbsorbingObject, AnisotropicObject, Object
 from .sources import GaussianPlaneSource, LineSource, PlaneSource, PointSource, SoftArbitraryPointSource
@@ -30,5 +31,6 @@ __all__ = [
     "Grid", "PML", "PeriodicBoundary", "DomainBorderPML", "Object", "AbsorbingObject",
     "AnisotropicObject", "PointSource", "LineSource", "PlaneSource", "GaussianPlaneSource",
     "SoftArbitraryPointSource", "LineDetector", "BlockDetector", "CurrentDetector", "PlaneDetector",
-    "DFTPlaneDetector", "backend", "set_backend", "adjoint", "constants", "waveforms", "conversions",
+    "DFTPlaneDetector", "FrequencyRoutines", "backend", "set_backend", "adjoint", "constants", "waveforms",
+    "conversions",
 ]

@@ -11,12 +11,12 @@ import os
 LIB_NAME = "libfdtd_gb300.so"
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), LIB_NAME)
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_BOUNDARIES = 9
 
 FLOAT32, FLOAT32C, FLOAT64 = 0, 1, 2
 BOUNDARY_PML, BOUNDARY_PERIODIC = 0, 1
-ITEM_OBJECT, ITEM_ABSORBING, ITEM_ANISOTROPIC, ITEM_SOFT, ITEM_HARD = 0, 1, 2, 3, 4
+ITEM_OBJECT, ITEM_ABSORBING, ITEM_ANISOTROPIC, ITEM_SOFT, ITEM_HARD, ITEM_FEEDBACK = 0, 1, 2, 3, 4, 5
 STATS_STATIC_MAX_ROWS = 1024  # FDTD_STATS_STATIC_MAX_ROWS
 
 STATUS = {
@@ -47,6 +47,7 @@ class ItemDesc(ctypes.Structure):
         ("lo", c_int32 * 3), ("hi", c_int32 * 3),
         ("weight", ctypes.c_double),
         ("coef", c_void_p * 3),
+        ("aux", c_int32), ("reserved", c_int32),
     ]
 
 
@@ -75,6 +76,8 @@ class GridDesc(ctypes.Structure):
         ("n_probe_cells", c_int32), ("probe_cells", c_void_p),
         ("n_dft", c_int32), ("dft", ctypes.POINTER(DftDesc)),
         ("n_phase_columns", c_int32),
+        ("n_current_cells", c_int32), ("current_cells", c_void_p),
+        ("grid_spacing", ctypes.c_double),
     ]
 
 
@@ -84,6 +87,7 @@ class RunArgs(ctypes.Structure):
         ("wave", c_void_p), ("phase", c_void_p),
         ("trace_E", c_void_p), ("trace_H", c_void_p),
         ("trace_capacity", c_int64), ("record_E", c_int64), ("record_H", c_int64),
+        ("trace_I", c_void_p), ("record_I", c_int64), ("step0", c_int64),
     ]
 
 

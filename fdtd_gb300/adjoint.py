@@ -38,7 +38,7 @@ import torch
 
 from . import _native
 from .boundaries import PML
-from .detectors import DFTPlaneDetector
+from .detectors import CurrentDetector, DFTPlaneDetector
 from .objects import AnisotropicObject, Object, AbsorbingObject
 
 
@@ -55,6 +55,10 @@ class _Runner:
                 raise ValueError(f"{o!r} is not registered on this grid")
             if isinstance(o, AbsorbingObject) or not isinstance(o, Object):
                 raise NotImplementedError("design objects must be Object or AnisotropicObject instances")
+        for src in grid.sources:
+            if hasattr(src, "current_detector"):
+                raise NotImplementedError("the adjoint does not transpose the current feedback of a "
+                                          "SoftArbitraryPointSource")
         self.grid = grid
         self.n = int(n_steps)
         if self.n < 1:
@@ -114,6 +118,8 @@ class _Runner:
         eng.check_status()
         self.trace_dets, self.dft_dets, outs = [], [], []
         for i, det in enumerate(g.detectors):
+            if isinstance(det, CurrentDetector):
+                continue  # records only, not differentiable outputs
             if isinstance(det, DFTPlaneDetector):
                 self.dft_dets.append(det)
                 outs.append(det.dft.clone())
@@ -128,6 +134,8 @@ class _Runner:
         out, k = {}, 0
         for i, det in enumerate(self.grid.detectors):
             name = _det_name(det, i)
+            if isinstance(det, CurrentDetector):
+                continue
             if isinstance(det, DFTPlaneDetector):
                 out[name] = {"dft": flat[k]}
                 k += 1
@@ -151,6 +159,8 @@ class _Runner:
         k = 0
         gdft = []
         for det in g.detectors:
+            if isinstance(det, CurrentDetector):
+                continue
             if isinstance(det, DFTPlaneDetector):
                 gg = grads[k]
                 k += 1

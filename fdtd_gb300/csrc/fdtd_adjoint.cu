@@ -13,6 +13,7 @@ static long box_cells(const ItemK &o) {
 
 static int validate(const Plan &p, const fdtd_adjoint_args *a) {
     if (a->n_steps < 0 || (a->parity != 0 && a->parity != 1)) return FDTD_ERR_ARGUMENT;
+    if (p.has_feedback) return FDTD_ERR_UNSUPPORTED;  // no transpose of the current feedback
     if (!a->lam_E || !a->lam_H) return FDTD_ERR_ARGUMENT;
     if (p.adj_V > 1 && (!aligned16(a->lam_E) || !aligned16(a->lam_H))) return FDTD_ERR_ARGUMENT;
     if ((a->curl || a->grad) && a->n_objects != p.n_objects) return FDTD_ERR_ARGUMENT;

@@ -94,6 +94,7 @@ static ItemK to_item(const fdtd_item_desc &d) {
     it.bnz = d.hi[2] - d.lo[2];
     it.weight = d.weight;
     for (int q = 0; q < 3; ++q) it.coef[q] = d.coef[q];
+    it.aux = d.aux;
     return it;
 }
 
@@ -114,7 +115,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (comp != (d->E_lo != nullptr) || comp != (d->H_lo != nullptr)) return FDTD_ERR_ARGUMENT;
     if (d->n_boundaries < 0 || d->n_boundaries > FDTD_MAX_BOUNDARIES) return FDTD_ERR_ARGUMENT;
     if (d->n_objects < 0 || d->n_sources_E < 0 || d->n_sources_H < 0 || d->n_columns < 0 ||
-        d->n_probe_cells < 0 || d->n_dft < 0 || d->n_phase_columns < 0 || d->x_chunk < 0)
+        d->n_probe_cells < 0 || d->n_dft < 0 || d->n_phase_columns < 0 || d->x_chunk < 0 ||
+        d->n_current_cells < 0 || (d->n_current_cells && !d->current_cells))
         return FDTD_ERR_ARGUMENT;
     if ((d->n_objects && !d->objects) || (d->n_sources_E && !d->sources_E) || (d->n_sources_H && !d->sources_H) ||
         (d->n_probe_cells && !d->probe_cells) || (d->n_dft && !d->dft))
@@ -125,6 +127,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     GridK &g = p.k;
     memset(&g, 0, sizeof(g));
     p.precision = d->precision;
+    p.has_feedback = 0;
+    p.n_current = 0;
     g.nx = d->nx;
     g.ny = d->ny;
     g.nz = d->nz;
@@ -416,7 +420,16 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         const int begin = (int)items.size();
         for (int q = 0; q < cnt; ++q) {
             const fdtd_item_desc &s = src[q];
-            if (s.kind != FDTD_ITEM_SOFT && s.kind != FDTD_ITEM_HARD) return FDTD_ERR_ARGUMENT;
+            if (s.kind != FDTD_ITEM_SOFT && s.kind != FDTD_ITEM_HARD && s.kind != FDTD_ITEM_FEEDBACK)
+                return FDTD_ERR_ARGUMENT;
+            if (s.kind == FDTD_ITEM_FEEDBACK) {
+                // E side only, one cell, a current-probe point, a grid spacing
+                if (side != 0 || s.aux < 0 || s.aux >= d->n_current_cells || !(d->grid_spacing > 0.0))
+                    return FDTD_ERR_ARGUMENT;
+                if (s.hi[0] - s.lo[0] != 1 || s.hi[1] - s.lo[1] != 1 || s.hi[2] - s.lo[2] != 1)
+                    return FDTD_ERR_ARGUMENT;
+                p.has_feedback = 1;
+            }
             if (!box_ok(s.lo, s.hi, d->nx, d->ny, d->nz) || s.comp < 0 || s.comp > 2) return FDTD_ERR_ARGUMENT;
             if (s.column < 0 || s.column >= d->n_columns) return FDTD_ERR_ARGUMENT;
             if (s.kind == FDTD_ITEM_SOFT && (s.hi[0] - s.lo[0] != 1 || s.hi[1] - s.lo[1] != 1 || s.hi[2] - s.lo[2] != 1))
@@ -470,7 +483,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             if (touches_periodic_plane(cit[q], periodic_axes, n)) return false;
         return true;
     };
-    g.fuse_src_E = can_fuse(srcE0, d->n_sources_E) ? 1 : 0;
+    // feedback sources read the current on the device: all E sources run as
+    // epilogue kernels then, in order
+    g.fuse_src_E = (!p.has_feedback && can_fuse(srcE0, d->n_sources_E)) ? 1 : 0;
     g.fuse_src_H = can_fuse(srcH0, d->n_sources_H) ? 1 : 0;
 
     // epilogue source launches and soft runs
@@ -485,10 +500,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         while (q < last) {
             int e = q + 1;
             while (e < last && items[e].source == items[q].source) ++e;
-            if (items[q].kind == FDTD_ITEM_HARD) {
+            if (items[q].kind == FDTD_ITEM_HARD || items[q].kind == FDTD_ITEM_FEEDBACK) {
                 for (int h = q; h < e; ++h) {
                     EpiOp op{};
-                    op.kind = EPI_HARD;
+                    op.kind = items[q].kind == FDTD_ITEM_HARD ? EPI_HARD : EPI_FEEDBACK;
                     op.item = h;
                     ops.push_back(op);
                 }
@@ -517,9 +532,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     build_csr(t, items, srcE0, d->n_sources_E, se_off, se_idx);
     build_csr(t, items, srcH0, d->n_sources_H, sh_off, sh_idx);
 
-    // probes and DFT boxes
+    // probes, current probes and DFT boxes
     p.n_probe = d->n_probe_cells;
     p.probe_cells = d->probe_cells;
+    p.n_current = d->n_current_cells;
+    p.current_cells = d->current_cells;
+    p.grid_spacing = d->grid_spacing;
     for (int q = 0; q < d->n_dft; ++q) {
         const fdtd_dft_desc &dd = d->dft[q];
         if (!box_ok(dd.lo, dd.hi, d->nx, d->ny, d->nz) || dd.n_freq < 1 || !dd.acc || dd.phase_offset < 0 ||
@@ -589,7 +607,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     p.stats_ctas = 152 * 4;
     p.launches_per_step = 2 + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
-                          (int)p.dft.size();
+                          (p.n_current > 0 ? 1 : 0) + (int)p.dft.size();
     return FDTD_OK;
 }
 

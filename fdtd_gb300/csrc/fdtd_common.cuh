@@ -34,6 +34,7 @@ struct ItemK {
     int bny, bnz;
     double weight;
     const void *coef[3];
+    int aux;  // FDTD_ITEM_FEEDBACK: its point in the current-probe list
 };
 
 // Everything a half-step kernel needs, passed by value.

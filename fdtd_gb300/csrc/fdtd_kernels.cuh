@@ -337,6 +337,70 @@ __global__ void k_hard_box(const GridK g, int item, const double *wave, int fiel
     }
 }
 
+// Feedback source (SoftArbitraryPointSource.update_E, fdtd/sources.py:600-629):
+// output = input + impedance * I_prev (only for impedance > 0), then
+// E[comp] += output / grid_spacing; I_prev is the source's current-probe point
+// after the previous H half, 0 at step 0 (iprev = null).
+template <class P>
+__global__ void k_feedback(const GridK g, int item, const double *wave, const typename P::T *iprev, double du) {
+    using T = typename P::T;
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const ItemK &s = g.items[item];
+    T *E = (T *)g.E;
+    T *Elo = (T *)g.Elo;
+    const size_t at = 3 * (((size_t)s.lo[0] * g.ny + s.lo[1]) * g.nz + s.lo[2]) + s.comp;
+    const T in = (T)wave[s.column];
+    const T cur = iprev ? iprev[s.aux] : T(0);
+    T out = in;
+    if (s.weight > 0.0) {
+        if constexpr (sizeof(T) == 8) out = __dadd_rn(in, __dmul_rn((T)s.weight, cur));
+        else out = in + (T)s.weight * cur;
+    }
+    T v;
+    if constexpr (sizeof(T) == 8) v = __ddiv_rn(out, (T)du);
+    else v = out / (T)du;
+    T x = E[at], lo = T(0);
+    if constexpr (P::COMP) lo = Elo[at];
+    P::add_prod(x, lo, v, T(1));
+    P::finish(x, lo);
+    E[at] = x;
+    if constexpr (P::COMP) Elo[at] = lo;
+}
+
+// Current probes (CurrentDetector.single_point_current, fdtd/detectors.py:404-464):
+// out[p] = I at cells[p] from H, with the reference's arithmetic order, its
+// running accumulation of the second y term, and negative neighbour indices
+// wrapping to the far side of the grid as Python indexing does.
+template <class T>
+__global__ void k_current(const T *__restrict__ H, const int64_t *__restrict__ cells, int n, int nx, int ny, int nz,
+                          double du_d, T *out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const long c = cells[p];
+    const int px = (int)(c / ((long)ny * nz)), py = (int)((c / nz) % ny), pz = (int)(c % nz);
+    const int xm = px > 0 ? px - 1 : nx - 1, ym = py > 0 ? py - 1 : ny - 1, zm = pz > 0 ? pz - 1 : nz - 1;
+    auto h = [&](int i, int j, int k, int comp) { return H[3 * (((size_t)i * ny + j) * nz + k) + comp]; };
+    const T du = (T)du_d;
+    T cur1, cur2;
+    if constexpr (sizeof(T) == 8) {
+        double cv1 = __dmul_rn(__dsub_rn(h(px, ym, pz, 0), h(px, py, pz, 0)), du);
+        double cv2 = __dmul_rn(__dsub_rn(h(px, py, pz, 1), h(xm, py, pz, 1)), du);
+        cur1 = __dadd_rn(cv1, cv2);
+        cv1 = __dmul_rn(__dsub_rn(h(px, ym, zm, 0), h(px, py, zm, 0)), du);
+        cv2 = __dadd_rn(cv2, __dmul_rn(__dsub_rn(h(px, py, zm, 1), h(xm, py, zm, 1)), du));
+        cur2 = __dadd_rn(cv1, cv2);
+        out[p] = __ddiv_rn(__dadd_rn(cur1, cur2), 2.0);
+    } else {
+        T cv1 = (h(px, ym, pz, 0) - h(px, py, pz, 0)) * du;
+        T cv2 = (h(px, py, pz, 1) - h(xm, py, pz, 1)) * du;
+        cur1 = cv1 + cv2;
+        cv1 = (h(px, ym, zm, 0) - h(px, py, zm, 0)) * du;
+        cv2 = cv2 + (h(px, py, zm, 1) - h(xm, py, zm, 1)) * du;
+        cur2 = cv1 + cv2;
+        out[p] = (cur1 + cur2) / T(2);
+    }
+}
+
 // Detector sampling: out[p][c] = F[cells[p]][c].
 template <class T>
 __global__ void k_probe(const T *__restrict__ F, const int64_t *__restrict__ cells, int n, T *out) {

@@ -52,7 +52,8 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
 }
 
 template <class P>
-static void launch_epilogue(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
+static void launch_epilogue(Plan &p, bool is_E, const double *wave, cudaStream_t st,
+                            const typename P::T *iprev = nullptr) {
     using T = typename P::T;
     const std::vector<EpiOp> &ops = is_E ? p.epi_E : p.epi_H;
     const GridK &g = p.k;
@@ -92,6 +93,10 @@ static void launch_epilogue(Plan &p, bool is_E, const double *wave, cudaStream_t
             }
             case EPI_HARD: {
                 k_hard_box<P><<<grid_stride_blocks(1L << 20), kThreads, 0, st>>>(g, op.item, wave, is_E ? 0 : 1);
+                break;
+            }
+            case EPI_FEEDBACK: {
+                k_feedback<P><<<1, 32, 0, st>>>(g, op.item, wave, iprev, p.grid_spacing);
                 break;
             }
         }
@@ -188,6 +193,11 @@ static int run_impl(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *ca
     if (detect && !p.dft.empty() && a->phase == nullptr && a->n_steps > 0 && a->half != 2)
         return FDTD_ERR_ARGUMENT;
     const bool probe = detect && p.n_probe > 0;
+    if (!detect && p.has_feedback) return FDTD_ERR_UNSUPPORTED;  // the currents drive the sources
+    const bool current = detect && p.n_current > 0;
+    if (current && (a->trace_I == nullptr || a->record_I < 0 ||
+                    (a->half != 1 && a->record_I + a->n_steps > a->trace_capacity)))
+        return FDTD_ERR_RANGE;
     if (probe) {
         if (a->half != 2 && (a->trace_E == nullptr || a->record_E < 0 ||
                              a->record_E + a->n_steps > a->trace_capacity))
@@ -210,8 +220,12 @@ static int run_impl(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *ca
             }
         }
         if (a->half != 2) {
+            // the current of the previous H half, for feedback sources
+            const T *iprev = nullptr;
+            if (current && a->step0 + s > 0 && a->record_I + s - 1 >= 0)
+                iprev = (const T *)a->trace_I + (a->record_I + s - 1) * p.n_current;
             launch_fused<P>(p, true, wave, st);
-            launch_epilogue<P>(p, true, wave, st);
+            launch_epilogue<P>(p, true, wave, st, iprev);
             if (probe)
                 k_probe<T><<<pblocks, kThreads, 0, st>>>((const T *)g.E, p.probe_cells, p.n_probe,
                                                         (T *)a->trace_E + (a->record_E + s) * 3 * p.n_probe);
@@ -229,6 +243,10 @@ static int run_impl(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *ca
             if (probe)
                 k_probe<T><<<pblocks, kThreads, 0, st>>>((const T *)g.H, p.probe_cells, p.n_probe,
                                                         (T *)a->trace_H + (a->record_H + s) * 3 * p.n_probe);
+            if (current)
+                k_current<T><<<(p.n_current + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                    (const T *)g.H, p.current_cells, p.n_current, g.nx, g.ny, g.nz, p.grid_spacing,
+                    (T *)a->trace_I + (a->record_I + s) * p.n_current);
         }
         const int rc = check_launch<P>();
         if (rc != FDTD_OK) return rc;

@@ -11,13 +11,13 @@
 
 namespace fdtd {
 
-enum EpiKind { EPI_COPY = 0, EPI_SLAB = 1, EPI_SOFT = 2, EPI_HARD = 3, EPI_PML = 4 };
+enum EpiKind { EPI_COPY = 0, EPI_SLAB = 1, EPI_SOFT = 2, EPI_HARD = 3, EPI_PML = 4, EPI_FEEDBACK = 5 };
 
 struct EpiOp {
     int kind;
     int axis;       // EPI_COPY
     int slab;       // EPI_SLAB (correction only), EPI_PML (auxiliary update and correction)
-    int item;       // EPI_HARD
+    int item;       // EPI_HARD, EPI_FEEDBACK
     int run_begin;  // EPI_SOFT
     int run_count;
 };
@@ -40,6 +40,10 @@ struct Plan {
     const int2 *runs;  // device, soft-source runs for EPI_SOFT
     int n_probe;
     const int64_t *probe_cells;
+    int n_current;                  // current-probe points (CurrentDetector)
+    int has_feedback;               // an FDTD_ITEM_FEEDBACK source exists
+    const int64_t *current_cells;
+    double grid_spacing;
     std::vector<fdtd_dft_desc> dft;
     int n_columns, n_phase_columns;
     void *dev_mem;     // the plan's own device tables

@@ -241,8 +241,40 @@ class DFTPlaneDetector(_Detector):
 
 
 class CurrentDetector(_Detector):
-    """Loop-current detector (fdtd/detectors.py:284-496).  Not supported by the
-    gb300 backend (it serves the SoftArbitraryPointSource impedance feature)."""
+    """Current around a point after every H half step (fdtd/detectors.py:284-496).
+
+    For every point of the index block (inclusive ranges like BlockDetector)
+    the device computes the reference's ``single_point_current``: the loop
+    integral of H around the z edge in the planes z and z-1, averaged, with the
+    reference's arithmetic order (including its running sum of the second
+    y term) and Python's wrap-around of the index -1.  ``det.I`` holds one
+    record per step of shape (nx, ny, nz) (the array form of the reference's
+    nested lists)."""
+
+    def __init__(self, name=None):
+        super().__init__(name=name)
+        del self.E, self.H
+        self._frozen = {"I": []}
+        self.orientation = None
+        self.I = TraceList(self, "I")
 
     def _register_grid(self, grid, x, y, z):
-        raise NotImplementedError("CurrentDetector is not supported by the gb300 backend")
+        if LineDetector._all_lists(x, y, z):
+            self.x, self.y, self.z = list(x), list(y), list(z)
+        else:
+            lo, hi = LineDetector._ranges(grid, x, y, z)
+            self.x, self.y, self.z = ([int(v) for v in np.arange(l, h + 1)] for l, h in zip(lo, hi))
+        self._rec_shape = (len(self.x), len(self.y), len(self.z))
+        self._finish_register(grid)
+
+    def _point_lists(self):
+        return np.meshgrid(np.asarray(self.x, np.int64), np.asarray(self.y, np.int64),
+                           np.asarray(self.z, np.int64), indexing="ij")
+
+    def detector_values(self):
+        """Outputs of the detector, {'I': records}."""
+        return {"I": self.I}
+
+    def __str__(self):
+        return (f"    {repr(self)}\n        @ x=[{self.x[0]}, ... , {self.x[-1]}], y=[{self.y[0]}, ... , "
+                f"{self.y[-1]}], z=[{self.z[0]}, ... , {self.z[-1]}]\n")

@@ -23,7 +23,7 @@ import torch
 
 from . import _native
 from .boundaries import PML, PeriodicBoundary
-from .detectors import DFTPlaneDetector
+from .detectors import CurrentDetector, DFTPlaneDetector
 
 _PRECISION = {"float32": _native.FLOAT32, "float32c": _native.FLOAT32C, "float64": _native.FLOAT64}
 
@@ -73,11 +73,13 @@ class Engine:
         self.plan = None
         self._key = None
         self._keep = []
-        self.trace_E = self.trace_H = None
+        self.trace_E = self.trace_H = self.trace_I = None
         self.capacity = 0
-        self.rec_E = self.rec_H = 0
+        self.rec_E = self.rec_H = self.rec_I = 0
         self.n_probe = 0
+        self.n_current = 0
         self.det_ranges = {}
+        self.cur_ranges = {}
         self.dfts = []
         self.n_phase = 0
         self._wave_stage = _PinnedStager()
@@ -140,15 +142,17 @@ class Engine:
                                "invalid")
 
     def _freeze_traces(self):
-        for det, (p0, p1) in self.det_ranges.items():
-            for field in ("E", "H"):
-                live = self.detector_records(det, field)
-                if live is not None and live.shape[0]:
-                    det._frozen[field].append(live.clone())
-            det._engine = None
+        for ranges, fields in ((self.det_ranges, ("E", "H")), (self.cur_ranges, ("I",))):
+            for det in ranges:
+                for field in fields:
+                    live = self.detector_records(det, field)
+                    if live is not None and live.shape[0]:
+                        det._frozen[field].append(live.clone())
+                det._engine = None
         self.det_ranges = {}
-        self.trace_E = self.trace_H = None
-        self.capacity = self.rec_E = self.rec_H = 0
+        self.cur_ranges = {}
+        self.trace_E = self.trace_H = self.trace_I = None
+        self.capacity = self.rec_E = self.rec_H = self.rec_I = 0
 
     def _destroy(self):
         if self.plan is not None:
@@ -219,29 +223,10 @@ class Engine:
         d.objects = objs
         keep.append(objs)
 
-        itemsE, itemsH = [], []
-        self.sources = list(g.sources)
-        for col, s in enumerate(self.sources):
-            if not hasattr(s, "_items"):
-                raise NotImplementedError(f"source {type(s).__name__} is not supported by the gb300 backend")
-            for field, kind, comp, lo, hi, w in s._items():
-                it = _native.ItemDesc()
-                it.kind = _native.ITEM_SOFT if kind == "soft" else _native.ITEM_HARD
-                it.comp, it.column, it.source = comp, col, col
-                it.lo[:] = list(lo)
-                it.hi[:] = list(hi)
-                it.weight = w
-                (itemsE if field == "E" else itemsH).append(it)
-        arrE = (_native.ItemDesc * max(1, len(itemsE)))(*itemsE)
-        arrH = (_native.ItemDesc * max(1, len(itemsH)))(*itemsH)
-        d.n_sources_E, d.sources_E = len(itemsE), arrE
-        d.n_sources_H, d.sources_H = len(itemsH), arrH
-        d.n_columns = len(self.sources)
-        keep.extend([arrE, arrH])
-
-        cells = []
-        self.n_probe = 0
+        cells, ccells = [], []
+        self.n_probe = self.n_current = 0
         self.det_ranges = {}
+        self.cur_ranges = {}
         self.dfts = []
         dfts = []
         nph = 0
@@ -256,6 +241,12 @@ class Engine:
                 nph += dd.n_freq
                 dfts.append(dd)
                 self.dfts.append(det)
+            elif isinstance(det, CurrentDetector):
+                c = det._probe_cells()
+                self.cur_ranges[det] = (self.n_current, self.n_current + c.size)
+                self.n_current += c.size
+                ccells.append(c)
+                det._engine = self
             elif hasattr(det, "_probe_cells"):
                 c = det._probe_cells()
                 self.det_ranges[det] = (self.n_probe, self.n_probe + c.size)
@@ -268,11 +259,43 @@ class Engine:
             probe = torch.as_tensor(np.concatenate(cells), dtype=torch.int64, device=g._device)
             keep.append(probe)
             d.n_probe_cells, d.probe_cells = self.n_probe, probe.data_ptr()
+        if self.n_current:
+            cur = torch.as_tensor(np.concatenate(ccells), dtype=torch.int64, device=g._device)
+            keep.append(cur)
+            d.n_current_cells, d.current_cells = self.n_current, cur.data_ptr()
+        d.grid_spacing = g.grid_spacing
         arrD = (_native.DftDesc * max(1, len(dfts)))(*dfts)
         d.n_dft, d.dft = len(dfts), arrD
         d.n_phase_columns = nph
         self.n_phase = nph
         keep.append(arrD)
+
+        itemsE, itemsH = [], []
+        self.sources = list(g.sources)
+        for col, s in enumerate(self.sources):
+            if not hasattr(s, "_items"):
+                raise NotImplementedError(f"source {type(s).__name__} is not supported by the gb300 backend")
+            for field, kind, comp, lo, hi, w in s._items():
+                it = _native.ItemDesc()
+                it.kind = {"soft": _native.ITEM_SOFT, "hard": _native.ITEM_HARD,
+                           "feedback": _native.ITEM_FEEDBACK}[kind]
+                if kind == "feedback":
+                    det = s.current_detector
+                    if det not in self.cur_ranges:
+                        raise RuntimeError("a SoftArbitraryPointSource needs its current detector in grid.detectors")
+                    it.aux = self.cur_ranges[det][0]
+                it.comp, it.column, it.source = comp, col, col
+                it.lo[:] = list(lo)
+                it.hi[:] = list(hi)
+                it.weight = w
+                (itemsE if field == "E" else itemsH).append(it)
+        arrE = (_native.ItemDesc * max(1, len(itemsE)))(*itemsE)
+        arrH = (_native.ItemDesc * max(1, len(itemsH)))(*itemsH)
+        d.n_sources_E, d.sources_E = len(itemsE), arrE
+        d.n_sources_H, d.sources_H = len(itemsH), arrH
+        d.n_columns = len(self.sources)
+        keep.extend([arrE, arrH])
+
 
         plan = ctypes.c_void_p()
         _native.check(lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan)), "fdtd_plan_create")
@@ -288,12 +311,20 @@ class Engine:
         cap = max(need, 2 * self.capacity, 16)
         newE = torch.empty((cap, self.n_probe, 3), dtype=g._dtype, device=g._device)
         newH = torch.empty((cap, self.n_probe, 3), dtype=g._dtype, device=g._device)
+        newI = torch.empty((cap, self.n_current), dtype=g._dtype, device=g._device)
         if self.trace_E is not None:
             newE[: self.rec_E].copy_(self.trace_E[: self.rec_E])
             newH[: self.rec_H].copy_(self.trace_H[: self.rec_H])
-        self.trace_E, self.trace_H, self.capacity = newE, newH, cap
+            newI[: self.rec_I].copy_(self.trace_I[: self.rec_I])
+        self.trace_E, self.trace_H, self.trace_I, self.capacity = newE, newH, newI, cap
 
     def detector_records(self, det, field):
+        if field == "I":
+            rng = self.cur_ranges.get(det)
+            if rng is None or self.trace_I is None:
+                return None
+            p0, p1 = rng
+            return self.trace_I[: self.rec_I, p0:p1].reshape((self.rec_I,) + det._rec_shape)
         rng = self.det_ranges.get(det)
         buf = self.trace_E if field == "E" else self.trace_H
         if rng is None or buf is None:
@@ -346,13 +377,25 @@ class Engine:
         a.n_steps, a.half = n, half
         a.wave = wave.data_ptr() if wave is not None else None
         a.phase = phase.data_ptr() if phase is not None else None
-        if self.n_probe and detect:
+        a.step0 = q0
+        if (self.n_probe or self.n_current) and detect:
             need_E = self.rec_E + (n if half != 2 else 0)
-            need_H = self.rec_H + (n if half != 1 else 0)
+            need_H = max(self.rec_H, self.rec_I) + (n if half != 1 else 0)
             self._ensure_capacity(max(need_E, need_H))
             a.trace_E, a.trace_H = self.trace_E.data_ptr(), self.trace_H.data_ptr()
+            a.trace_I = self.trace_I.data_ptr()
             a.trace_capacity = self.capacity
-            a.record_E, a.record_H = self.rec_E, self.rec_H
+            a.record_E, a.record_H, a.record_I = self.rec_E, self.rec_H, self.rec_I
+            if half != 2:
+                # feedback sources: the current record each E half step reads
+                # (the record of the previous H half; none at step 0)
+                for src in self.sources:
+                    if hasattr(src, "current_detector") and src.current_detector in self.cur_ranges:
+                        det = src.current_detector
+                        frozen = sum(c.shape[0] for c in det._frozen["I"])
+                        for k in range(n):
+                            r = self.rec_I + k - 1
+                            src._steps.append((q0 + k, frozen + r if (q0 + k > 0 and r >= 0) else -1))
         stream = ctypes.c_void_p(torch.cuda.current_stream(g._device).cuda_stream)
         if capture is None:
             _native.check(lib.fdtd_run(self.plan, ctypes.byref(a), stream), "fdtd_run")
@@ -365,11 +408,12 @@ class Engine:
             c.curl = arr
             _native.check(lib.fdtd_run_capture(self.plan, ctypes.byref(a), ctypes.byref(c), stream),
                           "fdtd_run_capture")
-        if self.n_probe and detect:
+        if (self.n_probe or self.n_current) and detect:
             if half != 2:
                 self.rec_E += n
             if half != 1:
                 self.rec_H += n
+                self.rec_I += n
 
     def run_capture(self, n, curls, detectors):
         """n full steps from time_steps_passed capturing curl_H on object boxes

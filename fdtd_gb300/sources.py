@@ -271,13 +271,82 @@ class GaussianPlaneSource(PlaneSource):
 
 
 class SoftArbitraryPointSource:
-    """Voltage-driven point source with a current detector feedback loop
-    (fdtd/sources.py:504-643).  Not supported by the gb300 backend: its
-    per-step host feedback (the detected current sets the next voltage) is
-    outside the fused time step."""
+    """Voltage-driven point source with a current feedback loop
+    (fdtd/sources.py:504-643).
 
-    def __init__(self, waveform_array, name=None, impedance=0.0):
-        self.waveform_array, self.name, self.impedance = waveform_array, name, impedance
+    At every E half step q the device adds ``output / grid_spacing`` to E_z at
+    the point, output = input + impedance * I (the impedance term only when
+    impedance > 0), input = waveform_array[q] (0 past its end) and I the
+    current its own CurrentDetector measured after the previous H half step
+    (0 at step 0).  The current is read on the device, so the feedback costs
+    no host round trip.  ``input_voltage`` and ``source_voltage`` give the
+    reference's per-step records ``[[[v]]]``, rebuilt from the waveform and
+    the detector's current records with the same float64 expressions.
+
+    Registration differs from the reference in two ways: a failing
+    registration leaves nothing in ``grid.sources`` (the reference appends
+    first), and a named source names its detector ``<name>_I`` (the reference
+    raises UnboundLocalError for a named source, fdtd/sources.py:592-595)."""
+
+    def __init__(self, waveform_array, name: str = None, impedance: float = 0.0):
+        self.grid = None
+        self.name = name
+        self.current_detector = None
+        self.waveform_array = waveform_array
+        self.impedance = impedance
+        self._steps = []  # per E half: (step index, index of the current record it used or -1)
 
     def _register_grid(self, grid, x, y, z):
-        raise NotImplementedError("SoftArbitraryPointSource is not supported by the gb300 backend")
+        from .detectors import CurrentDetector
+
+        try:
+            (x,), (y,), (z,) = x, y, z
+        except (TypeError, ValueError):
+            raise ValueError("a point source should be placed on a single grid cell.")
+        if self.name is not None and hasattr(grid, self.name):
+            raise ValueError(f"The grid already has an attribute with name {self.name}")
+        self.x, self.y, self.z = grid._handle_tuple((x, y, z))
+        self.grid = grid
+        grid.sources.append(self)
+        if self.name is not None:
+            setattr(grid, self.name, self)
+        self.current_detector = CurrentDetector(name=None if self.name is None else self.name + "_I")
+        grid[x, y, z] = self.current_detector
+        grid._invalidate()
+
+    def _value(self, q):
+        """input_voltage at step q (fdtd/sources.py:605-609)."""
+        w = self.waveform_array
+        return float(w[q]) if q < np.shape(w)[0] else 0.0
+
+    def _items(self):
+        return [("E", "feedback", 2, (self.x, self.y, self.z), (self.x + 1, self.y + 1, self.z + 1),
+                 float(self.impedance))]
+
+    def _voltages(self):
+        ins, outs = [], []
+        I = self.current_detector.I
+        for q, r in self._steps:
+            vin = self._value(q)
+            cur = float(I[r].reshape(-1)[0]) if r >= 0 else 0.0
+            vout = vin + self.impedance * cur if self.impedance > 0 else vin
+            ins.append([[[vin]]])
+            outs.append([[[vout]]])
+        return ins, outs
+
+    @property
+    def input_voltage(self):
+        """Per-step waveform input, [[[v]]] records (fdtd/sources.py:628)."""
+        return self._voltages()[0]
+
+    @property
+    def source_voltage(self):
+        """Per-step output voltage incl. the impedance term, [[[v]]] records
+        (fdtd/sources.py:629)."""
+        return self._voltages()[1]
+
+    def __repr__(self):
+        return f"{self.__class__.__name__}()"
+
+    def __str__(self):
+        return f"    {repr(self)}\n        @ x={self.x}, y={self.y}, z={self.z}\n"

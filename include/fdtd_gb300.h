@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 1
+#define FDTD_ABI_VERSION 2
 #define FDTD_MAX_BOUNDARIES 9 /* six PML slabs and three periodic axes */
 
 typedef void *fdtd_stream_t; /* a cudaStream_t */
@@ -92,7 +92,11 @@ typedef enum {
     FDTD_ITEM_ANISOTROPIC = 2, /* E += courant * (coef0 @ curlH), coef0 [cell][3][3]
                                   (fdtd/objects.py:254-269) */
     FDTD_ITEM_SOFT = 3,        /* F[comp] += weight * wave[column] (PointSource, LineSource) */
-    FDTD_ITEM_HARD = 4         /* F[comp]  = weight * wave[column] (PlaneSource) */
+    FDTD_ITEM_HARD = 4,        /* F[comp]  = weight * wave[column] (PlaneSource) */
+    FDTD_ITEM_FEEDBACK = 5     /* E[comp] += (wave[column] + weight * I) / grid_spacing, I the
+                                  current of current-probe point `aux` after the previous H
+                                  half (0 at step 0); the weight term only when weight > 0
+                                  (SoftArbitraryPointSource.update_E, fdtd/sources.py:600-629) */
 } fdtd_item_kind;
 
 /* An object box or a source box/point.  Object coefficient arrays are
@@ -104,8 +108,10 @@ typedef struct {
     int32_t source;   /* sources: index in grid.sources (fixes the order) */
     int32_t lo[3];    /* first cell (x, y, z) */
     int32_t hi[3];    /* one past the last cell (x, y, z) */
-    double weight;    /* sources: amplitude or profile weight */
+    double weight;    /* sources: amplitude or profile weight; feedback: source impedance */
     const void *coef[3];
+    int32_t aux;      /* FDTD_ITEM_FEEDBACK: index of its point in current_cells */
+    int32_t reserved;
 } fdtd_item_desc;
 
 /* Running DFT of E on a box: acc[f][cell][c] += E[cell][c] * (phase_re + i*phase_im),
@@ -153,6 +159,9 @@ typedef struct {
     int32_t n_dft;
     const fdtd_dft_desc *dft;         /* HOST array */
     int32_t n_phase_columns;          /* width of one DFT phase row (pairs) */
+    int32_t n_current_cells;          /* current-probe points (CurrentDetector), all detectors */
+    const int64_t *current_cells;     /* [n_current_cells] linear cell index */
+    double grid_spacing;              /* metres (current probes, feedback sources) */
 } fdtd_grid_desc;
 
 typedef struct fdtd_plan fdtd_plan;
@@ -169,6 +178,11 @@ typedef struct {
     int64_t trace_capacity;
     int64_t record_E;      /* row of trace_E written by the first E half */
     int64_t record_H;
+    void *trace_I;         /* [capacity][n_current_cells] currents after H halves
+                              (CurrentDetector.detect_H, fdtd/detectors.py:404-480) */
+    int64_t record_I;      /* row of trace_I written by the first H half */
+    int64_t step0;         /* time_steps_passed at the first step (feedback sources use the
+                              previous current only after step 0) */
 } fdtd_run_args;
 
 /* Build a plan for a registered grid (replaces the per-step dispatch of

@@ -835,6 +835,87 @@ class BlockDetector(LineDetector):
         self.H.append(self.grid.H[np.ix_(self.x, self.y, self.z)])
 
 
+class CurrentDetector:
+    """Loop current around a point after each H half step,
+    fdtd/detectors.py:284-496 (single_point_current :404-464).  Index ranges
+    are inclusive like BlockDetector; each record is an (nx, ny, nz) array,
+    the array form of the reference's nested lists."""
+
+    def __init__(self, name=None):
+        self.name = name
+        self.I = []
+
+    def _attach(self, grid, x, y, z):
+        r = _detector_ranges(grid, x, y, z)
+        if r is None:
+            self.x, self.y, self.z = x, y, z
+        else:
+            lo, hi = r
+            self.x, self.y, self.z = ([int(v) for v in np.arange(l, h + 1)] for l, h in zip(lo, hi))
+        self.grid = grid
+        grid.detectors.append(self)
+        _named(grid, self)
+
+    def _point(self, px, py, pz):
+        # the reference's order, its running sum of the second y term, and
+        # numpy's wrap-around of index -1
+        H, du = self.grid.H, self.grid.grid_spacing
+        cv1 = (H[px, py - 1, pz, 0] - H[px, py, pz, 0]) * du
+        cv2 = (H[px, py, pz, 1] - H[px - 1, py, pz, 1]) * du
+        c1 = cv1 + cv2
+        cv1 = (H[px, py - 1, pz - 1, 0] - H[px, py, pz - 1, 0]) * du
+        cv2 += (H[px, py, pz - 1, 1] - H[px - 1, py, pz - 1, 1]) * du
+        c2 = cv1 + cv2
+        return (c1 + c2) / 2.0
+
+    def sample_E(self):
+        pass
+
+    def sample_H(self):
+        self.I.append(np.array([[[self._point(px, py, pz) for pz in self.z] for py in self.y] for px in self.x]))
+
+    def detector_values(self):
+        return {"I": self.I}
+
+
+class SoftArbitraryPointSource:
+    """Voltage-driven point source with current feedback, fdtd/sources.py:504-643:
+    E_z += (input + impedance * I_prev) / grid_spacing at the point, I_prev the
+    last record of its own CurrentDetector (0 at step 0).  A named source names
+    its detector <name>_I (the reference fails for named sources)."""
+
+    def __init__(self, waveform_array, name=None, impedance=0.0):
+        self.name = name
+        self.waveform_array = waveform_array
+        self.impedance = impedance
+        self.input_voltage, self.source_voltage = [], []
+
+    def _attach(self, grid, x, y, z):
+        try:
+            (x,), (y,), (z,) = x, y, z
+        except (TypeError, ValueError):
+            raise ValueError("a point source should be placed on a single grid cell.")
+        self.grid = grid
+        self.x, self.y, self.z = (grid._handle_distance(v) for v in (x, y, z))
+        grid.sources.append(self)
+        _named(grid, self)
+        self.current_detector = CurrentDetector(name=None if self.name is None else self.name + "_I")
+        grid[x, y, z] = self.current_detector
+
+    def inject_E(self):  # fdtd/sources.py:600-629
+        g = self.grid
+        q = g.time_steps_passed
+        vin = self.waveform_array[q] if q < self.waveform_array.shape[0] else 0.0
+        cur = self.current_detector.I[-1][0][0][0] if q > 0 else 0.0
+        vout = vin + self.impedance * cur if self.impedance > 0 else vin
+        g.E[self.x, self.y, self.z, 2] += vout / g.grid_spacing
+        self.input_voltage.append([[[vin]]])
+        self.source_voltage.append([[[vout]]])
+
+    def inject_H(self):
+        pass
+
+
 def _half_open_box(grid, x, y, z):
     out = []
     for s, n in zip((x, y, z), grid.shape):

@@ -108,6 +108,25 @@ def g_domain_pml(fd):
     return grid, 30, run_steps
 
 
+def g_saps(fd):
+    """SoftArbitraryPointSource with a source impedance (the current measured
+    by its own CurrentDetector feeds back into the next E half step), a
+    separate CurrentDetector block, a conducting plate and a line detector in
+    a PML box with millimetre cells (the setting of the reference's impedance
+    test, tests/test_antenna_impedance.py).  The impedance, 0.2, keeps the
+    feedback loop stable: in the reference's field units the loop gain grows
+    with the impedance and at 1 or more the fields grow without bound."""
+    grid = fd.Grid((14, 12, 12), grid_spacing=1e-3)
+    fd.DomainBorderPML(grid, border_cells=3)
+    grid[4:10, 4:8, 5:6] = fd.AbsorbingObject(permittivity=1.0, conductivity=1e6, name="plate")
+    t = np.arange(60) * grid.time_step
+    wave = np.exp(-((t - 25 * grid.time_step) ** 2) / (2 * (6 * grid.time_step) ** 2))
+    grid[7, 6, 7] = fd.SoftArbitraryPointSource(wave, impedance=0.2)
+    grid[5:7, 3:5, 8] = fd.CurrentDetector(name="current")
+    grid[:, 6, 7] = fd.LineDetector(name="line")
+    return grid, 60, run_steps
+
+
 SCENES = {
     "c1": g_c1,
     "c2": g_c2,
@@ -117,6 +136,7 @@ SCENES = {
     "2d": g_2d,
     "manual": g_manual,
     "domain_pml": g_domain_pml,
+    "saps": g_saps,
 }
 
 
@@ -124,8 +144,15 @@ def snapshot(grid):
     """Final fields and every detector trace as float64 numpy arrays."""
     out = {"E": _np(grid.E), "H": _np(grid.H), "q": np.array(grid.time_steps_passed)}
     for i, det in enumerate(grid.detectors):
+        if hasattr(det, "I"):  # CurrentDetector
+            out[f"det{i}_I"] = np.stack([_np(c) for c in det.I]) if len(det.I) else np.zeros((0,))
+            continue
         out[f"det{i}_E"] = np.stack([_np(e) for e in det.E]) if len(det.E) else np.zeros((0,))
         out[f"det{i}_H"] = np.stack([_np(h) for h in det.H]) if len(det.H) else np.zeros((0,))
+    for j, src in enumerate(grid.sources):
+        if hasattr(src, "source_voltage"):  # SoftArbitraryPointSource
+            out[f"src{j}_Vin"] = _np(src.input_voltage)
+            out[f"src{j}_Vout"] = _np(src.source_voltage)
     return out
 
 

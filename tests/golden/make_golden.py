@@ -2,7 +2,7 @@
 
 Usage (needs a checkout of the reference; nothing else in the repository reads it):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [scene ...]
 
 The reference imports matplotlib for plotting only; a no-op stand-in from
 ``tests/golden/mplstub`` is put on ``sys.path`` first.  Outputs:
@@ -31,10 +31,24 @@ def load_reference(path):
 
     fdtd.set_backend("numpy")
     fdtd.DomainBorderPML = fdtd.boundaries.DomainBorderPML
+    fdtd.SoftArbitraryPointSource = fdtd.sources.SoftArbitraryPointSource
     return fdtd
 
 
-def main(ref_path):
+def fourier_fixture(fdtd, grid):
+    """FrequencyRoutines (fdtd/fourier.py) outputs on the 'saps' scene."""
+    from fdtd.fourier import FrequencyRoutines
+
+    src = next(s for s in grid.sources if isinstance(s, fdtd.SoftArbitraryPointSource))
+    f_z, z = FrequencyRoutines(grid, src).impedance()
+    f_i, s_i = FrequencyRoutines(grid, grid.current).FFT()
+    arr = np.sin(np.arange(37) * 0.3)
+    f_a, s_a = FrequencyRoutines(grid, arr).FFT()
+    return dict(imp_freqs=np.asarray(f_z), imp=np.asarray(z), cur_freqs=np.asarray(f_i), cur_fft=np.asarray(s_i),
+                arr=arr, arr_freqs=np.asarray(f_a), arr_fft=np.asarray(s_a))
+
+
+def main(ref_path, only=None):
     fdtd = load_reference(ref_path)
     sys.path.insert(0, REPO)
     sys.path.insert(0, HERE)
@@ -46,13 +60,18 @@ def main(ref_path):
     np.savez(os.path.join(HERE, "ref_curls.npz"), E=E0, curl_E=curl_E(E0), H=H1, curl_H=curl_H(H1),
              reference_version=fdtd.__version__)
     for name, build in golden_scenes.SCENES.items():
+        if only and name not in only:
+            continue
         grid, steps, drive = build(fdtd)
         drive(grid, steps)
         snap = golden_scenes.snapshot(grid)
         snap["steps"] = np.array(steps)
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **snap)
         print(name, {k: v.shape for k, v in snap.items()})
+        if name == "saps":
+            np.savez_compressed(os.path.join(HERE, "ref_saps_fourier.npz"), **fourier_fixture(fdtd, grid))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # optional further arguments: only these scenes
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:] or None)

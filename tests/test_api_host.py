@@ -161,6 +161,12 @@ def test_registration_matches_oracle(fd, name):
         if hasattr(oobj, "absorption_factor"):
             assert np.array_equal(obj.absorption_factor.cpu().numpy(), oobj.absorption_factor)
     for s, os_ in zip(g.sources, o.sources):
+        if isinstance(s, fd.SoftArbitraryPointSource):
+            assert (s.x, s.y, s.z, s.impedance) == (os_.x, os_.y, os_.z, os_.impedance)
+            for q in (0, 3, 59, 60, 100):
+                vin = os_.waveform_array[q] if q < os_.waveform_array.shape[0] else 0.0
+                assert s._value(q) == vin
+            continue
         assert s.period == os_.period
         if isinstance(s, fd.LineSource):
             assert np.array_equal(np.asarray(s.profile), os_.profile)
@@ -193,8 +199,25 @@ def test_no_cpu_time_step(fd):
 
 def test_unsupported_components(grid, fd):
     with pytest.raises(NotImplementedError):
-        grid[4, 4, 4] = fd.CurrentDetector()
-    with pytest.raises(NotImplementedError):
-        grid[4, 4, 4] = fd.SoftArbitraryPointSource(np.zeros(4))
-    with pytest.raises(NotImplementedError):
         fd.Object(permittivity=1 + 1j)
+
+
+def test_soft_arbitrary_point_source_registration(grid, fd):
+    """fdtd/sources.py:562-598: one cell; the source registers its own
+    CurrentDetector at the cell (named <name>_I here; the reference raises
+    UnboundLocalError for a named source)."""
+    with pytest.raises(ValueError):
+        grid[4:6, 4, 4] = fd.SoftArbitraryPointSource(np.zeros(4))
+    assert not grid.sources
+    src = fd.SoftArbitraryPointSource(np.ones(4), impedance=50.0, name="port")
+    grid[4, 5, 6] = src
+    assert grid.port is src and grid.sources == [src]
+    det = src.current_detector
+    assert grid.port_I is det and det in grid.detectors
+    assert (det.x, det.y, det.z) == ([4], [5], [6]) and det._rec_shape == (1, 1, 1)
+    assert (src.x, src.y, src.z) == (4, 5, 6)
+    assert src._value(3) == 1.0 and src._value(4) == 0.0
+    cd = fd.CurrentDetector(name="loop")
+    grid[2:4, 3:5, 7] = cd  # inclusive ranges like BlockDetector
+    assert (cd.x, cd.y, cd.z) == ([2, 3, 4], [3, 4, 5], [7]) and not hasattr(cd, "E")
+    assert cd.detector_values()["I"] is cd.I
