@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(kThreads) k_adj_H(const GridK g, const AdjAux 
     const int xa = blockIdx.z * g.XC;
     const int xb = min(nx, xa + g.XC);
     const bool act = (j < ny) && (k0 < nz);
-    const T c = courant_of<T>(g);
+    const T c = material_courant<T>(g);  // courant * material factor
     const T *LH = (const T *)g.H;
     T *LE = (T *)g.E;
     const T *__restrict__ MU = (const T *)g.imu;
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(kThreads) k_adj_E(const GridK g, const AdjAux 
     const int xa = blockIdx.z * g.XC;
     const int xb = min(nx, xa + g.XC);
     const bool act = (j < ny) && (k0 < nz);
-    const T c = courant_of<T>(g);
+    const T c = material_courant<T>(g);  // courant * material factor
     const T *LE = (const T *)g.E;
     T *LH = (T *)g.H;
     const T *__restrict__ IE = (const T *)g.ie;
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kThreads) k_adj_slab(const GridK g, const AdjA
     const int a = S.axis, th = S.th;
     const int n0 = a == 0 ? th : g.nx, n1 = a == 1 ? th : g.ny, n2 = a == 2 ? th : g.nz;
     const long total = (long)n0 * n1 * n2;
-    const T c = courant_of<T>(g);
+    const T c = material_courant<T>(g);  // courant * material factor
     const T *L = (const T *)(IS_E ? g.E : g.H);  // lam_E (E half) or lam_H (H half), read
     T *O = (T *)(IS_E ? g.H : g.E);              // the adjoint field updated
     const T *__restrict__ M = (const T *)(IS_E ? g.ie : g.imu);
@@ -593,7 +593,7 @@ __global__ void k_adj_slab_inc(const GridK g, int s, T *aux) {
     const int n0 = a == 0 ? S.th : g.nx, n1 = a == 1 ? S.th : g.ny, n2 = a == 2 ? S.th : g.nz;
     const int p2 = a == 2 ? S.thp : g.nz;
     const long total = (long)n0 * n1 * n2;
-    const T c = courant_of<T>(g);
+    const T c = material_courant<T>(g);  // courant * material factor
     const T *L = (const T *)(IS_E ? g.E : g.H);
     const T *M = (const T *)(IS_E ? g.ie : g.imu);
     const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;

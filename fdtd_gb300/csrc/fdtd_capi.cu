@@ -140,6 +140,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.Hlo = d->H_lo;
     g.ie = d->inv_eps;
     g.imu = d->inv_mu;
+    if (d->materials_scaled != 0 && d->materials_scaled != 1) return FDTD_ERR_ARGUMENT;
+    if (d->materials_scaled && d->precision != FDTD_FLOAT64) return FDTD_ERR_UNSUPPORTED;
+    g.scaled = d->materials_scaled;
 
     // boundaries: PML slabs in order, periodic axes, the first periodic position
     int first_periodic = d->n_boundaries;

@@ -207,14 +207,14 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
                 // phi[(a+1)%3] = -p0, phi[(a+2)%3] = +p1 (fdtd/boundaries.py:457-459, 485-487);
                 // explicit branches keep the field values in registers
                 if (a == 0) {
-                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::mul(c, m[3 * v + 1]), -p0[v]);
-                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::mul(c, m[3 * v + 2]), p1[v]);
+                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::cm(c, m[3 * v + 1]), -p0[v]);
+                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::cm(c, m[3 * v + 2]), p1[v]);
                 } else if (a == 1) {
-                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::mul(c, m[3 * v + 2]), -p0[v]);
-                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::mul(c, m[3 * v]), p1[v]);
+                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::cm(c, m[3 * v + 2]), -p0[v]);
+                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::cm(c, m[3 * v]), p1[v]);
                 } else {
-                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::mul(c, m[3 * v]), -p0[v]);
-                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::mul(c, m[3 * v + 1]), p1[v]);
+                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::cm(c, m[3 * v]), -p0[v]);
+                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::cm(c, m[3 * v + 1]), p1[v]);
                 }
             }
         }
@@ -264,9 +264,9 @@ __device__ __forceinline__ void thread_E(const GridK &g, const double *__restric
         const T cu0 = d[3][v] - d[5][v];
         const T cu1 = d[4][v] - d[1][v];
         const T cu2 = d[0][v] - d[2][v];
-        P::add_prod(e[3 * v], el[3 * v], P::mul(c, m[3 * v]), cu0);
-        P::add_prod(e[3 * v + 1], el[3 * v + 1], P::mul(c, m[3 * v + 1]), cu1);
-        P::add_prod(e[3 * v + 2], el[3 * v + 2], P::mul(c, m[3 * v + 2]), cu2);
+        P::add_prod(e[3 * v], el[3 * v], P::cm(c, m[3 * v]), cu0);
+        P::add_prod(e[3 * v + 1], el[3 * v + 1], P::cm(c, m[3 * v + 1]), cu1);
+        P::add_prod(e[3 * v + 2], el[3 * v + 2], P::cm(c, m[3 * v + 2]), cu2);
         if (ob0 < ob1)
             apply_objects<P>(g, i, j, k, c, cu0, cu1, cu2, e[3 * v], e[3 * v + 1], e[3 * v + 2], el[3 * v],
                              el[3 * v + 1], el[3 * v + 2], ob0, ob1);
@@ -306,9 +306,9 @@ __device__ __forceinline__ void thread_H(const GridK &g, const double *__restric
         d[3][v] = (j < g.ny - 1) ? ej[3 * v + 2] - ez_ : T(0);
         d[4][v] = (k < g.nz - 1) ? nkx - ex_ : T(0);
         d[5][v] = (k < g.nz - 1) ? nky - ey_ : T(0);
-        P::sub_prod(h[3 * v], hl[3 * v], P::mul(c, m[3 * v]), d[3][v] - d[5][v]);
-        P::sub_prod(h[3 * v + 1], hl[3 * v + 1], P::mul(c, m[3 * v + 1]), d[4][v] - d[1][v]);
-        P::sub_prod(h[3 * v + 2], hl[3 * v + 2], P::mul(c, m[3 * v + 2]), d[0][v] - d[2][v]);
+        P::sub_prod(h[3 * v], hl[3 * v], P::cm(c, m[3 * v]), d[3][v] - d[5][v]);
+        P::sub_prod(h[3 * v + 1], hl[3 * v + 1], P::cm(c, m[3 * v + 1]), d[4][v] - d[1][v]);
+        P::sub_prod(h[3 * v + 2], hl[3 * v + 2], P::cm(c, m[3 * v + 2]), d[0][v] - d[2][v]);
     }
     if (slabs) apply_pml<P, V, false>(g, i, j, k0, c, d, m, h, hl, src, slabs);
 #pragma unroll

@@ -61,6 +61,7 @@ struct GridK {
     int psi_off[kMaxSlabs], psi_pitch[kMaxSlabs];
     int coef_off[kMaxSlabs];  // per slab: offset (values) of its b/c tables in shared memory
     int coef_values;          // values of all staged b/c tables (0: tables are read from global)
+    int scaled;               // ie / imu hold courant * inverse material (float64 plans)
 };
 
 template <class T>
@@ -74,6 +75,13 @@ __device__ __forceinline__ double courant_of<double>(const GridK &g) {
     return g.courant;
 }
 
+// Multiplier of the inverse materials in a product courant * material:
+// 1 when the plan's material arrays already hold that product.
+template <class T>
+__device__ __forceinline__ T material_courant(const GridK &g) {
+    return g.scaled ? T(1) : courant_of<T>(g);
+}
+
 // ---------------------------------------------------------------------------
 // Precision policies.  The float64 policy reproduces the reference's numpy
 // operation order with explicitly rounded operations (no fused multiply-add),
@@ -85,6 +93,8 @@ struct PF64 {
     static constexpr bool COMP = false;
     static constexpr int V = 2;
     __device__ __forceinline__ static T mul(T a, T b) { return __dmul_rn(a, b); }
+    // courant * inverse material of a cell (the reference forms this product first)
+    __device__ __forceinline__ static T cm(T c, T m) { return __dmul_rn(c, m); }
     __device__ __forceinline__ static void add_prod(T &x, T &, T a, T b) {
         x = __dadd_rn(x, __dmul_rn(a, b));
     }
@@ -106,11 +116,19 @@ struct PF64 {
     __device__ __forceinline__ static void finish(T &, T &) {}
 };
 
+// float64 with the inverse materials already multiplied by the courant number
+// on the host (the same rounded products the reference forms), so the
+// kernels skip that product; GB300's float64 rate bounds these kernels.
+struct PF64S : PF64 {
+    __device__ __forceinline__ static T cm(T, T m) { return m; }
+};
+
 struct PF32 {
     using T = float;
     static constexpr bool COMP = false;
     static constexpr int V = 4;
     __device__ __forceinline__ static T mul(T a, T b) { return a * b; }
+    __device__ __forceinline__ static T cm(T c, T m) { return c * m; }
     __device__ __forceinline__ static void add_prod(T &x, T &, T a, T b) { x = fmaf(a, b, x); }
     __device__ __forceinline__ static void sub_prod(T &x, T &, T a, T b) { x = fmaf(-a, b, x); }
     __device__ __forceinline__ static void scale(T &x, T &, T r) { x = x * r; }
@@ -138,6 +156,7 @@ struct PF32C {
         e = (a - ap) + (b - bp);
     }
     __device__ __forceinline__ static T mul(T a, T b) { return a * b; }
+    __device__ __forceinline__ static T cm(T c, T m) { return c * m; }
     __device__ __forceinline__ static void add_prod(T &x, T &lo, T a, T b) {
         T p = a * b;
         T pe = fmaf(a, b, -p);

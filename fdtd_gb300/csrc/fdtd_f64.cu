@@ -3,9 +3,9 @@
 
 namespace fdtd {
 int run_f64(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaStream_t st) {
-    return run_impl<PF64>(p, a, cap, st);
+    return p.k.scaled ? run_impl<PF64S>(p, a, cap, st) : run_impl<PF64>(p, a, cap, st);
 }
-int prepare_tma_f64(Plan &p) { return prepare_tma_impl<PF64>(p); }
+int prepare_tma_f64(Plan &p) { return p.k.scaled ? prepare_tma_impl<PF64S>(p) : prepare_tma_impl<PF64>(p); }
 
 size_t tma_stage_bytes(int precision, int tile_rows) {
     switch (precision) {

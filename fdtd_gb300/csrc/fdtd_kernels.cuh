@@ -212,7 +212,7 @@ __global__ void k_slab_correct(const GridK g, int s) {
             l1 = Flo[3 * cell + t1];
             l2 = Flo[3 * cell + t2];
         }
-        const T c1 = P::mul(c, M[3 * cell + t1]), c2 = P::mul(c, M[3 * cell + t2]);
+        const T c1 = P::cm(c, M[3 * cell + t1]), c2 = P::cm(c, M[3 * cell + t2]);
         if (IS_E) {
             P::add_prod(x1, l1, c1, -p0);
             P::add_prod(x2, l2, c2, p1);
@@ -280,8 +280,8 @@ __global__ void __launch_bounds__(kThreads) k_pml_slab(const GridK g, int s) {
             l1 = Flo[at + t1];
             l2 = Flo[at + t2];
         }
-        pml_correct<P, IS_E>(x1, l1, P::mul(c, M[at + t1]), -p0);
-        pml_correct<P, IS_E>(x2, l2, P::mul(c, M[at + t2]), p1);
+        pml_correct<P, IS_E>(x1, l1, P::cm(c, M[at + t1]), -p0);
+        pml_correct<P, IS_E>(x2, l2, P::cm(c, M[at + t2]), p1);
         P::finish(x1, l1);
         P::finish(x2, l2);
         F[at + t1] = x1;

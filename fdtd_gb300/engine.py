@@ -73,6 +73,8 @@ class Engine:
         self.plan = None
         self._key = None
         self._keep = []
+        self._scaled = None
+        self._scaled_keys = [None, None]
         self.trace_E = self.trace_H = self.trace_I = None
         self.capacity = 0
         self.rec_E = self.rec_H = self.rec_I = 0
@@ -97,10 +99,25 @@ class Engine:
         g = self.grid
         key = self._state_key()
         if self.plan is not None and not g._dirty and key == self._key:
+            self._sync_scaled_materials()
             return
         self._build()
         self._key = self._state_key()
         g._dirty = False
+
+    # float64 plans read courant * inverse material (the products the
+    # reference forms first, rounded the same way) from arrays kept here; they
+    # follow in-place changes of the grid's materials before every launch
+    def _sync_scaled_materials(self):
+        g = self.grid
+        if self._scaled is None:
+            return
+        for src, dst, ver in zip((g._inverse_permittivity, g._inverse_permeability), self._scaled,
+                                 range(2)):
+            key = (id(src), src._version, g.courant_number)
+            if self._scaled_keys[ver] != key:
+                torch.mul(src, g.courant_number, out=dst)
+                self._scaled_keys[ver] = key
 
     def set_x_chunk(self, x_chunk):
         self.x_chunk = int(x_chunk)
@@ -187,8 +204,16 @@ class Engine:
         d.E, d.H = g._E.data_ptr(), g._H.data_ptr()
         d.E_lo = g._E_lo.data_ptr() if g._E_lo is not None else None
         d.H_lo = g._H_lo.data_ptr() if g._H_lo is not None else None
-        d.inv_eps = g._inverse_permittivity.data_ptr()
-        d.inv_mu = g._inverse_permeability.data_ptr()
+        if g.precision == "float64":
+            if self._scaled is None or self._scaled[0].shape != g._inverse_permittivity.shape:
+                self._scaled = (torch.empty_like(g._inverse_permittivity), torch.empty_like(g._inverse_permeability))
+            self._scaled_keys = [None, None]
+            self._sync_scaled_materials()
+            d.inv_eps, d.inv_mu = self._scaled[0].data_ptr(), self._scaled[1].data_ptr()
+            d.materials_scaled = 1
+        else:
+            d.inv_eps = g._inverse_permittivity.data_ptr()
+            d.inv_mu = g._inverse_permeability.data_ptr()
 
         if len(g.boundaries) > _native.MAX_BOUNDARIES:
             raise NotImplementedError("more boundaries than the gb300 backend supports")

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 2
+#define FDTD_ABI_VERSION 3
 #define FDTD_MAX_BOUNDARIES 9 /* six PML slabs and three periodic axes */
 
 typedef void *fdtd_stream_t; /* a cudaStream_t */
@@ -162,6 +162,10 @@ typedef struct {
     int32_t n_current_cells;          /* current-probe points (CurrentDetector), all detectors */
     const int64_t *current_cells;     /* [n_current_cells] linear cell index */
     double grid_spacing;              /* metres (current probes, feedback sources) */
+    int32_t materials_scaled;         /* FDTD_FLOAT64 only: 1 = inv_eps and inv_mu hold
+                                         courant * inverse_permittivity / permeability (the
+                                         products the reference forms first), so the kernels
+                                         skip that multiply; 0 = plain inverse materials */
 } fdtd_grid_desc;
 
 typedef struct fdtd_plan fdtd_plan;
