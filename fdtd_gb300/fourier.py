@@ -9,8 +9,10 @@ as the reference, pads with the last value to the same length
 records live on, returning torch tensors (as the reference does on its torch
 backends).  The reference's selections are kept as they are: ``FFT`` of a
 line or block detector transforms ``E[:][0][0][0]`` (one index of the first
-record, the reference's FIXME), and ``impedance`` divides the spectra where
-the current spectrum is non-zero, zero elsewhere.
+record, the reference's FIXME; for a block detector that is a (z, component)
+array, padded along its first axis and transformed along its last one, as
+numpy.pad and numpy.fft.fft do there), and ``impedance`` divides the spectra
+where the current spectrum is non-zero, zero elsewhere.
 
 One difference: with ``freq_window_tuple`` the reference's
 ``compute_frequencies`` reads undefined names and raises NameError
@@ -114,7 +116,7 @@ class FrequencyRoutines:
                                                    fft_num_bins_in_window=fft_num_bins_in_window,
                                                    fft_bin_freq_resolution=fft_bin_freq_resolution)
         input_data = _pad_edge(input_data, required_padding)
-        spectrum = torch.fft.fft(input_data, dim=0)
+        spectrum = torch.fft.fft(input_data)  # last axis, like numpy.fft.fft
         freqs, b, e = self.compute_frequencies(input_data.shape[0], self.grid.time_step,
                                                freq_window_tuple=freq_window_tuple)
         return freqs[b:e], spectrum[b:e]
