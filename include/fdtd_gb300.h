@@ -9,8 +9,11 @@
  * objects fdtd/objects.py:118-277, sources fdtd/sources.py:93-109,278-297,
  * 476-486, detectors fdtd/detectors.py:114-124,241-265).  This library
  * replaces that whole chain: one plan describes a registered grid, and each
- * E or H half step is one fused kernel pass over the grid (plus small plane
- * kernels where a periodic boundary forces a fixed order).
+ * E or H half step is one fused kernel pass over the grid, followed by small
+ * kernels where the reference's order requires them (PML slabs run on their
+ * own on large grids, periodic plane copies, sources on those planes or
+ * slabs, detector gathers).  A reverse-time adjoint (fdtd_run_capture,
+ * fdtd_adjoint_run) gives gradients with respect to object materials.
  *
  * Conventions
  *  - Every pointer inside a descriptor is a DEVICE pointer unless stated.
