@@ -45,8 +45,16 @@ UNIT = "Gcell-updates/s"
 # read inverse material, write field (3 components each); compensated adds the
 # read and write of the compensation term.  PML slab cells add the read and
 # write of their two auxiliaries.
-CELL_BYTES = {"float32": 48, "float32c": 72, "float64": 96}
+CELL_BYTES = {"float32": 48, "float32c": 72, "float64": 96}  # per cell and half step, full material arrays
 SLAB_BYTES = {"float32": 16, "float32c": 16, "float64": 32}
+MAT_BYTES = {"float32": 12, "float32c": 12, "float64": 24}  # the three material values of a cell
+
+
+def half_bytes(prec, layout):
+    """Algorithmic bytes per cell of one fused half step for a material layout
+    (None: full arrays, ("index", n): one byte, ("uniform", 1): nothing)."""
+    mat = MAT_BYTES[prec] if layout is None else (1 if layout[0] == "index" else 0)
+    return CELL_BYTES[prec] - MAT_BYTES[prec] + mat
 
 
 def parse():
@@ -62,6 +70,8 @@ def parse():
     p.add_argument("--tile-rows", type=int, default=0)
     p.add_argument("--stages", type=int, default=0)
     p.add_argument("--pml-mode", type=int, default=0, help="0 auto, 1 PML inside the fused pass, 2 slab kernels")
+    p.add_argument("--materials", type=int, default=0,
+                   help="0 compact material copies where possible (one-byte index or uniform), 1 full arrays")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-adjoint", action="store_true", help="skip the adjoint/forward timing (configs 4, 5)")
@@ -201,7 +211,7 @@ def build_grid(fd, scenes, prec, n, eps, args):
     g = scenes.c3(fd, n=n, pml=pml, eps=eps, detector=True)
     eng = g._ensure_engine()
     eng.set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages, x_chunk=args.x_chunk,
-                   pml_mode=args.pml_mode)
+                   pml_mode=args.pml_mode, materials=args.materials)
     return g, eng
 
 
@@ -248,8 +258,12 @@ def run_precision(prec, args, dist, fd, scenes, eps, want_halves, want_e2e, samp
         "trace": g.detector.E.tensor()[: args.warmup + args.steps].double().cpu(),
         "stats": g.field_stats(),
     }
-    algo = cells * CELL_BYTES[prec] + slab_cells(g) * SLAB_BYTES[prec]
-    out["algo_bytes_half"] = algo
+    layout = eng.compact_materials()
+    out["materials"] = {"E": layout[0], "H": layout[1]}
+    slabs = slab_cells(g) * SLAB_BYTES[prec]
+    out["algo_bytes"] = {"E": cells * half_bytes(prec, layout[0]) + slabs,
+                         "H": cells * half_bytes(prec, layout[1]) + slabs}
+    out["full_bytes_half"] = cells * CELL_BYTES[prec] + slabs
     if want_halves:
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
                 torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -428,7 +442,8 @@ def gb300_arm(args):
     peak, peak_kind = peaks()
     kern = max(main["half_ms"], key=main["half_ms"].get) if "half_ms" in main else "E"
     t_kern = main["half_ms"][kern] if "half_ms" in main else main["ms_per_step"] / 2
-    achieved = main["algo_bytes_half"] / (t_kern * 1e-3) / 1e9
+    algo_kern = main["algo_bytes"][kern]
+    achieved = algo_kern / (t_kern * 1e-3) / 1e9
     traffic = traffic_from_profile(precs[0], n)
     line = {
         "metric": METRIC,
@@ -461,7 +476,9 @@ def gb300_arm(args):
             "unit": "GB/s",
             "frac": achieved / peak,
             "peak_kind": f"{peak_kind} (STREAM-style copy, MEASURED_PEAKS.json hbm_gbs)",
-            "algo_bytes_per_launch": main["algo_bytes_half"],
+            "algo_bytes_per_launch": algo_kern,
+            "materials": main["materials"],
+            "full_array_equivalent_gbs": main["full_bytes_half"] / (t_kern * 1e-3) / 1e9,
             "traffic": traffic,
         },
         "gpu_launches": main["launches_per_step"] * args.steps,
@@ -472,8 +489,9 @@ def gb300_arm(args):
     if "float64" in res:
         f64 = res["float64"]
         line["fp64"] = {"value": f64["gcells"], "ms_per_step": f64["ms_per_step"],
-                        "hbm_frac": (f64["algo_bytes_half"] / (max(f64["half_ms"].values()) * 1e-3) / 1e9) / peak
-                        if "half_ms" in f64 else None}
+                        "hbm_frac": max(f64["algo_bytes"][h] / (f64["half_ms"][h] * 1e-3) / 1e9
+                                        for h in ("E", "H")) / peak if "half_ms" in f64 else None,
+                        "materials": f64["materials"]}
         if precs[0] == "float32":
             line["fp32_over_fp64"] = main["gcells"] / f64["gcells"]
         ref = f64["trace"]

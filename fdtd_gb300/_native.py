@@ -11,7 +11,7 @@ import os
 LIB_NAME = "libfdtd_gb300.so"
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), LIB_NAME)
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 MAX_BOUNDARIES = 9
 
 FLOAT32, FLOAT32C, FLOAT64 = 0, 1, 2
@@ -78,6 +78,8 @@ class GridDesc(ctypes.Structure):
         ("n_phase_columns", c_int32),
         ("n_current_cells", c_int32), ("current_cells", c_void_p),
         ("grid_spacing", ctypes.c_double), ("materials_scaled", c_int32),
+        ("eps_table", c_void_p), ("n_eps_table", c_int32), ("eps_index", c_void_p),
+        ("mu_table", c_void_p), ("n_mu_table", c_int32), ("mu_index", c_void_p),
     ]
 
 

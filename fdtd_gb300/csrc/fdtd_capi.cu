@@ -31,6 +31,9 @@ static int next_pow2(int v) {
 
 static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
 
+// Padded 4-value rows of the shared-memory material table of a staged pass.
+static int mat_lut_rows(int mat) { return mat == MAT_IDS ? 256 : (mat == MAT_UNIFORM ? 1 : 0); }
+
 static bool box_ok(const int32_t lo[3], const int32_t hi[3], int nx, int ny, int nz) {
     const int n[3] = {nx, ny, nz};
     for (int a = 0; a < 3; ++a)
@@ -143,6 +146,20 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (d->materials_scaled != 0 && d->materials_scaled != 1) return FDTD_ERR_ARGUMENT;
     if (d->materials_scaled && d->precision != FDTD_FLOAT64) return FDTD_ERR_UNSUPPORTED;
     g.scaled = d->materials_scaled;
+    // compact material copies: validated here, used only by the staged passes
+    int mat_want[2] = {MAT_FULL, MAT_FULL};
+    {
+        const void *tab[2] = {d->eps_table, d->mu_table};
+        const int nt[2] = {d->n_eps_table, d->n_mu_table};
+        const uint8_t *idx[2] = {d->eps_index, d->mu_index};
+        for (int q = 0; q < 2; ++q) {
+            if (nt[q] < 0 || nt[q] > 256) return FDTD_ERR_ARGUMENT;
+            if (nt[q] == 0) continue;
+            if (!tab[q] || (!idx[q] && nt[q] != 1)) return FDTD_ERR_ARGUMENT;
+            if (idx[q] && (d->nz % 16 != 0 || !aligned16(idx[q]))) continue;  // no index map: full arrays
+            mat_want[q] = idx[q] ? MAT_IDS : MAT_UNIFORM;
+        }
+    }
 
     // boundaries: PML slabs in order, periodic axes, the first periodic position
     int first_periodic = d->n_boundaries;
@@ -273,82 +290,124 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         t.V = vmax;
         if (d->tile_rows != 0 && d->tile_rows != 4 && d->tile_rows != 8 && d->tile_rows != 16)
             return FDTD_ERR_ARGUMENT;
-        // tile shapes: 32 threads along z x 8 (or 4) rows, or 16 x 16.  The
-        // 16-wide tile fits z extents that are a multiple of 16 V but not of
-        // 32 V (config 5: nz = 192) and needs one halo row per 16 rows; its
-        // stage holds the auxiliary rows of at most 4 slabs (64 lanes' worth)
-        int rows = d->tile_rows;
-        if (rows == 0) {
-            const long z32 = 32L * vmax, z16 = 16L * vmax;
-            const long waste32 = (d->nz + z32 - 1) / z32 * z32 - d->nz;
-            const long waste16 = (d->nz + z16 - 1) / z16 * z16 - d->nz;
-            rows = (waste16 < waste32 && ks <= 4) ? 16 : 8;
-        }
-        if (rows == 16 && ks > 4) {
-            if (d->variant == 2 && d->tile_rows == 16) return FDTD_ERR_UNSUPPORTED;
-            rows = 8;
-        }
-        t.TY = rows;
-        t.TZ = rows == 16 ? 16 : 32;
-        // stage layout: field tiles, then one PML auxiliary slot per group of
-        // slabs of one axis that never meet in the same tile (rows copied per stage)
-        const int Zc = t.TZ * t.V;
-        const size_t field = tma_stage_bytes(d->precision, t.TY);
-        struct Slot {
-            int axis;
-            size_t bytes;
-            std::vector<std::pair<int, int>> ranges;
-            size_t off;
+        // tile shapes: 32 threads along z x 8 (or 4) rows, or 16 x 16 (one
+        // halo row per 16 rows).  Stage layout of a tile height: field tiles, then one PML auxiliary
+        // slot per group of slabs of one axis that never meet in the same tile
+        // (rows copied per stage); returns the stage bytes and fills the slot
+        // offsets and pitches of the plan
+        const int lut_rows = std::max(mat_lut_rows(mat_want[0]), mat_lut_rows(mat_want[1]));
+        auto stage_layout = [&](int TY, int TZ) -> size_t {
+            const int Zc = TZ * t.V;
+            const size_t field = tma_stage_bytes(d->precision, TY, mat_want[0], mat_want[1]);
+            struct Slot {
+                int axis;
+                size_t bytes;
+                std::vector<std::pair<int, int>> ranges;
+                size_t off;
+            };
+            std::vector<Slot> slots;
+            int slot_of[kMaxSlabs] = {0};
+            for (int s = 0; s < ks; ++s) {
+                const SlabK &S = g.slab[s];
+                const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? TY : Zc);
+                const std::pair<int, int> rg(S.start / unit, (S.start + S.th - 1) / unit);
+                const int pitch = S.axis == 2 ? 2 * S.thp : 2 * Zc;
+                const size_t bytes = (size_t)TY * pitch * esize;
+                g.psi_pitch[s] = pitch;
+                int found = -1;
+                for (int q = 0; q < (int)slots.size() && found < 0; ++q) {
+                    if (slots[q].axis != S.axis) continue;
+                    bool disjoint = true;
+                    for (auto &o : slots[q].ranges)
+                        if (!(rg.second < o.first || o.second < rg.first)) disjoint = false;
+                    if (disjoint) found = q;
+                }
+                if (found < 0) {
+                    slots.push_back(Slot{S.axis, 0, {}, 0});
+                    found = (int)slots.size() - 1;
+                }
+                slots[found].ranges.push_back(rg);
+                slots[found].bytes = std::max(slots[found].bytes, bytes);
+                slot_of[s] = found;
+            }
+            size_t stage = field;
+            for (auto &sl : slots) {
+                sl.off = stage;
+                stage += (sl.bytes + 127) & ~(size_t)127;
+            }
+            for (int s = 0; s < ks; ++s) g.psi_off[s] = (int)slots[slot_of[s]].off;
+            return stage;
         };
-        std::vector<Slot> slots;
-        int slot_of[kMaxSlabs] = {0};
-        for (int s = 0; s < ks; ++s) {
-            const SlabK &S = g.slab[s];
-            const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? t.TY : Zc);
-            const std::pair<int, int> rg(S.start / unit, (S.start + S.th - 1) / unit);
-            const int pitch = S.axis == 2 ? 2 * S.thp : 2 * Zc;
-            const size_t bytes = (size_t)t.TY * pitch * esize;
-            g.psi_pitch[s] = pitch;
-            int found = -1;
-            for (int q = 0; q < (int)slots.size() && found < 0; ++q) {
-                if (slots[q].axis != S.axis) continue;
-                bool disjoint = true;
-                for (auto &o : slots[q].ranges)
-                    if (!(rg.second < o.first || o.second < rg.first)) disjoint = false;
-                if (disjoint) found = q;
-            }
-            if (found < 0) {
-                slots.push_back(Slot{S.axis, 0, {}, 0});
-                found = (int)slots.size() - 1;
-            }
-            slots[found].ranges.push_back(rg);
-            slots[found].bytes = std::max(slots[found].bytes, bytes);
-            slot_of[s] = found;
-        }
-        size_t stage = field;
-        for (auto &sl : slots) {
-            sl.off = stage;
-            stage += (sl.bytes + 127) & ~(size_t)127;
-        }
-        for (int s = 0; s < ks; ++s) g.psi_off[s] = (int)slots[slot_of[s]].off;
-        g.stage_bytes = (int)stage;
         int coef = 0;
         for (int s = 0; s < ks; ++s) {
             g.coef_off[s] = coef;
             coef += 2 * g.slab[s].th;
         }
         g.coef_values = (size_t)coef * esize <= 16384 ? coef : 0;
-        const size_t extra = (size_t)g.coef_values * esize + 128;
+        // shared memory after the ring: barriers, b/c tables, then (16-byte
+        // aligned) the material table of the pass: 256 padded rows for
+        // indices, so that every index byte reads inside it
+        const size_t extra = (size_t)g.coef_values * esize + (size_t)lut_rows * 4 * esize + 16 + 128;
+        const long per_sm = 228L * 1024;  // shared memory of one SM
+        auto smem_of = [&](size_t stage, int S) { return (size_t)S * stage + (size_t)S * 8 + extra; };
+        auto resident = [&](size_t smem) { return std::max(1, (int)(per_sm / (long)(smem + 1024))); };
+        // ring stages that let two CTAs share an SM (0 if fewer than 3 fit)
+        auto stages_for_two = [&](size_t stage) {
+            const long room = per_sm / 2 - 1024 - (long)extra;
+            const long S2 = std::min<long>(6, room / (long)(stage + 8));
+            return S2 >= 3 && smem_of(stage, (int)S2) <= (size_t)optin ? (int)S2 : 0;
+        };
+        // tile height.  Explicit: as asked (16 rows are 16 threads wide).
+        // Automatic: 16 x 16 tiles where they waste less of the z extent
+        // than 32-wide ones (config 5: nz = 192) and the stage holds their
+        // slab rows (at most 4 slabs, 64 lanes' worth); else 8 rows, or 4
+        // when only 4-row stages let two CTAs share an SM.  One CTA of 8 warps
+        // leaves the staged passes latency-bound once the per-cell bytes
+        // drop (one-byte material indices): two CTAs per SM measured 77 vs
+        // 67 Gcell/s on config 3 (float32) and 15.2 vs 12.6 (float64), and
+        // the same as one CTA with full material arrays
+        int rows = d->tile_rows;
+        if (rows == 16 && ks > 4) {
+            if (d->variant == 2) return FDTD_ERR_UNSUPPORTED;
+            rows = 8;
+        }
+        if (rows == 0) {
+            const long z32 = 32L * vmax, z16 = 16L * vmax;
+            const long waste32 = (d->nz + z32 - 1) / z32 * z32 - d->nz;
+            const long waste16 = (d->nz + z16 - 1) / z16 * z16 - d->nz;
+            if (waste16 < waste32 && ks <= 4) {
+                rows = 16;
+            } else {
+                rows = 8;
+                if (!stages_for_two(stage_layout(8, 32)) && stages_for_two(stage_layout(4, 32))) rows = 4;
+            }
+        }
+        t.TY = rows;
+        t.TZ = rows == 16 ? 16 : 32;
+        const size_t stage = stage_layout(t.TY, t.TZ);
+        g.stage_bytes = (int)stage;
         int S = d->stages;
-        if (S == 0) S = (int)std::max<long>(0, std::min<long>(6, ((long)optin - (long)extra) / (long)(stage + 8)));
-        const size_t smem = (size_t)S * stage + (size_t)S * 8 + extra;
+        if (S == 0) {
+            S = stages_for_two(stage);
+            if (S == 0) S = (int)std::max<long>(0, std::min<long>(6, ((long)optin - (long)extra) / (long)(stage + 8)));
+        }
+        const size_t smem = smem_of(stage, S);
         if (S < 2 || smem > (size_t)optin) {
             if (d->variant == 2) return FDTD_ERR_UNSUPPORTED;
             use_tma = false;  // automatic choice: too little shared memory, use the register kernels
         } else {
             g.stages = S;
-            ctas_per_sm = std::max(1, (int)((228L * 1024) / (long)(smem + 1024)));
+            ctas_per_sm = resident(smem);
             p.variant = 2;
+            g.mat_E = mat_want[0];
+            g.mat_H = mat_want[1];
+            g.mlut_E = d->eps_table;
+            g.mlut_H = d->mu_table;
+            g.nlut_E = g.mat_E == MAT_FULL ? 0 : d->n_eps_table;
+            g.nlut_H = g.mat_H == MAT_FULL ? 0 : d->n_mu_table;
+            g.lut_rows = lut_rows;
+            p.index_E = d->eps_index;
+            p.index_H = d->mu_index;
         }
     }
     if (!use_tma) {

@@ -38,6 +38,12 @@ struct ItemK {
 };
 
 // Everything a half-step kernel needs, passed by value.
+// Material modes of a staged pass: the inverse material read per cell as
+// three values (MAT_FULL), as a one-byte index into a small table of value
+// triples (MAT_IDS), or not at all when every cell has the same triple
+// (MAT_UNIFORM).  The values and the arithmetic are the same in every mode.
+constexpr int MAT_FULL = 0, MAT_IDS = 1, MAT_UNIFORM = 2;
+
 struct GridK {
     int nx, ny, nz;
     double courant;
@@ -55,13 +61,19 @@ struct GridK {
     int TZ, TY, XC;                  // threads along z, rows along y, planes along x per CTA
     int stages;                      // shared-memory ring depth of the staged (TMA) kernels
     int *status;                     // device error word (bit 0: a pipeline wait timed out)
-    // staged kernels: bytes of one stage, TMA bytes of the field tiles, and per
-    // slab the byte offset (in a stage) and row pitch (values) of its psi slot
-    int stage_bytes, field_tx;
+    // staged kernels: bytes of one stage, and per slab the byte offset (in a
+    // stage) and row pitch (values) of its psi slot
+    int stage_bytes;
     int psi_off[kMaxSlabs], psi_pitch[kMaxSlabs];
     int coef_off[kMaxSlabs];  // per slab: offset (values) of its b/c tables in shared memory
     int coef_values;          // values of all staged b/c tables (0: tables are read from global)
     int scaled;               // ie / imu hold courant * inverse material (float64 plans)
+    // staged passes: material mode of the E and H pass (MAT_FULL, MAT_IDS,
+    // MAT_UNIFORM) and the value-triple tables they index
+    int mat_E, mat_H;
+    const void *mlut_E, *mlut_H;
+    int nlut_E, nlut_H;
+    int lut_rows;  // padded 4-value rows reserved for the table in shared memory
 };
 
 template <class T>

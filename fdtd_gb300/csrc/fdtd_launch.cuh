@@ -20,16 +20,30 @@ static int check_launch() {
     return FDTD_OK;
 }
 
-template <class P, int TZ, int TY>
-static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
+template <class P, int TZ, int TY, int MAT>
+static void launch_tma_mat(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     const dim3 block(TZ, TY, 1);
     const CUtensorMap *m = p.maps;
     if (is_E)
-        k_update_E_tma<P, TZ, TY><<<p.grid, block, p.smem_bytes, st>>>(
+        k_update_E_tma<P, TZ, TY, MAT><<<p.grid, block, p.smem_bytes, st>>>(
             p.kf, wave, m[MAP_H_NBR], m[MAP_E_OWN], m[MAP_IE], m[P::COMP ? MAP_ELO : MAP_E_OWN]);
     else
-        k_update_H_tma<P, TZ, TY><<<p.grid, block, p.smem_bytes, st>>>(
+        k_update_H_tma<P, TZ, TY, MAT><<<p.grid, block, p.smem_bytes, st>>>(
             p.kf, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
+}
+
+template <class P, int TZ, int TY>
+static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
+    switch (is_E ? p.kf.mat_E : p.kf.mat_H) {
+        case MAT_IDS:
+            launch_tma_mat<P, TZ, TY, MAT_IDS>(p, is_E, wave, st);
+            break;
+        case MAT_UNIFORM:
+            launch_tma_mat<P, TZ, TY, MAT_UNIFORM>(p, is_E, wave, st);
+            break;
+        default:
+            launch_tma_mat<P, TZ, TY, MAT_FULL>(p, is_E, wave, st);
+    }
 }
 
 // Staged-kernel tile shapes (threads along z x rows): 32x8, 32x4, 16x16.
@@ -117,6 +131,21 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+// 2D view of the one-byte material indices: rows = nx*ny, row = nz bytes;
+// box = box_w bytes by box_rows rows.
+static bool encode_index_map(CUtensorMap *m, const void *base, const GridK &g, int box_w, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (enc == nullptr || base == nullptr) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)g.nz, (cuuint64_t)g.nx * g.ny};
+    cuuint64_t strides[1] = {(cuuint64_t)g.nz};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void *>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 // 2D view of an (nx, ny, nz, 3) field: rows = nx*ny, row = 3*nz values, as
 // 8-byte elements; box = box_w elements by box_rows rows.
 static bool encode_field_map(CUtensorMap *m, const void *base, const GridK &g, int esize, int box_w, int box_rows) {
@@ -132,6 +161,31 @@ static bool encode_field_map(CUtensorMap *m, const void *base, const GridK &g, i
     return r == CUDA_SUCCESS;
 }
 
+// Map of one pass's material tile: the full values, the indices, or none.
+template <class P, int TZ, int TY>
+static bool encode_material_map(CUtensorMap *m, int mat, const void *full, const void *index, const GridK &g) {
+    using G = StageGeom<typename P::T, TZ, TY, P::COMP>;
+    if (mat == MAT_FULL) return encode_field_map(m, full, g, (int)sizeof(typename P::T), G::boxO, TY);
+    if (mat == MAT_IDS) return encode_index_map(m, index, g, G::boxI, TY);
+    return true;
+}
+
+template <class P, int TZ, int TY, int MAT>
+static cudaError_t allow_smem(bool is_E, size_t bytes) {
+    if (is_E)
+        return cudaFuncSetAttribute(k_update_E_tma<P, TZ, TY, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)bytes);
+    return cudaFuncSetAttribute(k_update_H_tma<P, TZ, TY, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes);
+}
+
+template <class P, int TZ, int TY>
+static cudaError_t allow_smem_mode(int mat, bool is_E, size_t bytes) {
+    if (mat == MAT_IDS) return allow_smem<P, TZ, TY, MAT_IDS>(is_E, bytes);
+    if (mat == MAT_UNIFORM) return allow_smem<P, TZ, TY, MAT_UNIFORM>(is_E, bytes);
+    return allow_smem<P, TZ, TY, MAT_FULL>(is_E, bytes);
+}
+
 template <class P, int TZ, int TY>
 static int prepare_tma_rows(Plan &p) {
     using G = StageGeom<typename P::T, TZ, TY, P::COMP>;
@@ -141,20 +195,16 @@ static int prepare_tma_rows(Plan &p) {
               encode_field_map(&p.maps[MAP_E_NBR], g.E, g, es, G::boxN, TY + 1) &&
               encode_field_map(&p.maps[MAP_E_OWN], g.E, g, es, G::boxO, TY) &&
               encode_field_map(&p.maps[MAP_H_OWN], g.H, g, es, G::boxO, TY) &&
-              encode_field_map(&p.maps[MAP_IE], g.ie, g, es, G::boxO, TY) &&
-              encode_field_map(&p.maps[MAP_MU], g.imu, g, es, G::boxO, TY);
+              encode_material_map<P, TZ, TY>(&p.maps[MAP_IE], g.mat_E, g.ie, p.index_E, g) &&
+              encode_material_map<P, TZ, TY>(&p.maps[MAP_MU], g.mat_H, g.imu, p.index_H, g);
     if (ok && P::COMP)
         ok = encode_field_map(&p.maps[MAP_ELO], g.Elo, g, es, G::boxO, TY) &&
              encode_field_map(&p.maps[MAP_HLO], g.Hlo, g, es, G::boxO, TY);
     if (!ok) return FDTD_ERR_UNSUPPORTED;
-    p.k.field_tx = (int)G::txBytes;
     p.smem_bytes = (size_t)g.stages * g.stage_bytes + (size_t)g.stages * 8 +
-                   (size_t)g.coef_values * sizeof(typename P::T) + 128;
-    cudaError_t e = cudaFuncSetAttribute(k_update_E_tma<P, TZ, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)p.smem_bytes);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_update_H_tma<P, TZ, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)p.smem_bytes);
+                   ((size_t)g.coef_values + 4 * (size_t)g.lut_rows) * sizeof(typename P::T) + 16 + 128;
+    cudaError_t e = allow_smem_mode<P, TZ, TY>(g.mat_E, true, p.smem_bytes);
+    if (e == cudaSuccess) e = allow_smem_mode<P, TZ, TY>(g.mat_H, false, p.smem_bytes);
     if (e != cudaSuccess) {
         set_last_cuda_error((int)e);
         return FDTD_ERR_CUDA;
@@ -168,11 +218,28 @@ static int prepare_tma_impl(Plan &p) {
     return p.k.TY == 8 ? prepare_tma_rows<P, 32, 8>(p) : prepare_tma_rows<P, 32, 4>(p);
 }
 
+template <class P, int TZ, int TY>
+static size_t stage_bytes_mode(int mat) {
+    using T = typename P::T;
+    if (mat == MAT_IDS) return (size_t)StageGeom<T, TZ, TY, P::COMP, MAT_IDS>::stageBytes;
+    if (mat == MAT_UNIFORM) return (size_t)StageGeom<T, TZ, TY, P::COMP, MAT_UNIFORM>::stageBytes;
+    return (size_t)StageGeom<T, TZ, TY, P::COMP, MAT_FULL>::stageBytes;
+}
+
 template <class P>
-static size_t stage_bytes_of(int tile_rows) {
-    if (tile_rows == 16) return (size_t)StageGeom<typename P::T, 16, 16, P::COMP>::stageBytes;
-    return tile_rows == 8 ? (size_t)StageGeom<typename P::T, 32, 8, P::COMP>::stageBytes
-                          : (size_t)StageGeom<typename P::T, 32, 4, P::COMP>::stageBytes;
+static size_t stage_bytes_of(int tile_rows, int mat_E, int mat_H) {
+    size_t a, b;
+    if (tile_rows == 16) {
+        a = stage_bytes_mode<P, 16, 16>(mat_E);
+        b = stage_bytes_mode<P, 16, 16>(mat_H);
+    } else if (tile_rows == 8) {
+        a = stage_bytes_mode<P, 32, 8>(mat_E);
+        b = stage_bytes_mode<P, 32, 8>(mat_H);
+    } else {
+        a = stage_bytes_mode<P, 32, 4>(mat_E);
+        b = stage_bytes_mode<P, 32, 4>(mat_H);
+    }
+    return a > b ? a : b;
 }
 
 // n_steps full steps (or one half step).  With capture arguments: detectors

@@ -36,6 +36,7 @@ struct Plan {
     int variant;       // 1 register streaming, 2 TMA-staged
     size_t smem_bytes; // dynamic shared memory of the TMA-staged kernels
     CUtensorMap maps[MAP_COUNT];
+    const void *index_E, *index_H;  // one-byte material indices (MAT_IDS)
     std::vector<EpiOp> epi_E, epi_H;
     const int2 *runs;  // device, soft-source runs for EPI_SOFT
     int n_probe;
@@ -70,8 +71,9 @@ int run_f64(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *cap, cudaS
 int adjoint_f32(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st);
 int adjoint_f64(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st);
 
-// Stage size in bytes of the TMA-staged kernels for a precision and tile rows.
-size_t tma_stage_bytes(int precision, int tile_rows);
+// Stage size in bytes of the TMA-staged kernels for a precision, tile rows
+// and the material modes of the E and H passes (the larger of the two).
+size_t tma_stage_bytes(int precision, int tile_rows, int mat_E, int mat_H);
 // Tensor maps and the shared-memory attribute of the TMA-staged kernels.
 int prepare_tma_f32(Plan &p);
 int prepare_tma_f32c(Plan &p);

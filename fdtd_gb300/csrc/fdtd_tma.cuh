@@ -77,10 +77,11 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // Byte layout of the field part of one stage: the neighbour tile (TY+1 rows
-// of 3*Zc+4 values) then the own tiles (TY rows of 3*Zc values each),
-// 128-byte aligned.  The PML auxiliary slots follow at g.psi_off[s].  A tile
-// is TZ threads (V cells each) along z by TY rows.
-template <class T, int TZ, int TY, bool COMP>
+// of 3*Zc+4 values), the own field tile (TY rows of 3*Zc values), the own
+// material tile (values, indices or nothing) and, compensated, the own
+// compensation tile, each 128-byte aligned.  The PML auxiliary slots follow
+// at g.psi_off[s].  A tile is TZ threads (V cells each) along z by TY rows.
+template <class T, int TZ, int TY, bool COMP, int MAT = MAT_FULL>
 struct StageGeom {
     static constexpr int V = sizeof(T) == 4 ? 4 : 2;
     static constexpr int Zc = TZ * V;  // cells per tile row
@@ -88,15 +89,17 @@ struct StageGeom {
     static constexpr int pitchO = 3 * Zc;
     static constexpr int nbrBytes = (TY + 1) * pitchN * (int)sizeof(T);
     static constexpr int ownBytes = TY * pitchO * (int)sizeof(T);
-    static constexpr int nOwn = COMP ? 3 : 2;
+    static constexpr int matBytes = MAT == MAT_FULL ? ownBytes : (MAT == MAT_IDS ? TY * Zc : 0);
     static constexpr int al(int v) { return (v + 127) & ~127; }
     static constexpr int ownOff = al(nbrBytes);
-    static constexpr int ownStride = al(ownBytes);
-    static constexpr int stageBytes = ownOff + nOwn * ownStride;
-    static constexpr uint32_t txBytes = (uint32_t)(nbrBytes + nOwn * ownBytes);
-    // tensor-map boxes in 8-byte elements
+    static constexpr int matOff = ownOff + al(ownBytes);
+    static constexpr int loOff = matOff + al(matBytes);
+    static constexpr int stageBytes = loOff + (COMP ? al(ownBytes) : 0);
+    static constexpr uint32_t txBytes = (uint32_t)(nbrBytes + ownBytes + matBytes + (COMP ? ownBytes : 0));
+    // tensor-map boxes in 8-byte elements (fields, full materials) and bytes (indices)
     static constexpr int boxN = pitchN * (int)sizeof(T) / 8;
     static constexpr int boxO = pitchO * (int)sizeof(T) / 8;
+    static constexpr int boxI = Zc;
 };
 
 // Fill one stage for plane p (warp 0 of the CTA, all lanes).  The PML auxiliary rows of
@@ -107,7 +110,8 @@ template <class T, int TY>
 __device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, uint32_t bar, int p, bool with_psi,
                                            bool is_E, int k0c, int j0, int Zc, const CUtensorMap *tmN, int xN,
                                            int yN, const CUtensorMap *tmF, const CUtensorMap *tmM,
-                                           const CUtensorMap *tmL, bool comp, int xO, int ownOff, int ownStride) {
+                                           const CUtensorMap *tmL, bool comp, int xO, int xM, int mat,
+                                           uint32_t field_tx, int ownOff, int matOff, int loOff) {
     const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
     uint32_t bytes[2] = {0u, 0u};
     const void *srcp[2] = {nullptr, nullptr};
@@ -143,16 +147,18 @@ __device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, ui
         dst[h] = smem_u32(st + g.psi_off[s] + (size_t)rr * g.psi_pitch[s] * sizeof(T));
     }
     const uint32_t tot = __reduce_add_sync(0xffffffffu, bytes[0] + bytes[1]);
-    if (lane == 0) mbar_expect_tx(bar, (uint32_t)g.field_tx + tot);
+    if (lane == 0) mbar_expect_tx(bar, field_tx + tot);
     __syncwarp();
 #pragma unroll
     for (int h = 0; h < 2; ++h)
         if (bytes[h]) bulk_copy_g2s(dst[h], srcp[h], bytes[h], bar);
     if (lane == 0) {
+        const int yO = yN + (is_E ? 1 : 0);
         tma_load_2d(smem_u32(st), tmN, xN, yN, bar);
-        tma_load_2d(smem_u32(st + ownOff), tmF, xO, yN + (is_E ? 1 : 0), bar);
-        tma_load_2d(smem_u32(st + ownOff + ownStride), tmM, xO, yN + (is_E ? 1 : 0), bar);
-        if (comp) tma_load_2d(smem_u32(st + ownOff + 2 * ownStride), tmL, xO, yN + (is_E ? 1 : 0), bar);
+        tma_load_2d(smem_u32(st + ownOff), tmF, xO, yO, bar);
+        if (mat == MAT_FULL) tma_load_2d(smem_u32(st + matOff), tmM, xO, yO, bar);
+        else if (mat == MAT_IDS) tma_load_2d(smem_u32(st + matOff), tmM, xM, yO, bar);
+        if (comp) tma_load_2d(smem_u32(st + loOff), tmL, xO, yO, bar);
     }
 }
 
@@ -168,13 +174,68 @@ __device__ __forceinline__ void stage_coef_tables(const GridK &g, T *tab, bool i
     }
 }
 
-template <class P, int TZ, int TY>
+// Copy the n material value triples of a half step into the padded 4-value
+// rows of the shared-memory table; rows n .. rows-1 are zero (all threads).
+template <class T>
+__device__ __forceinline__ void stage_material_table(const void *lut, int n, int rows, T *dst) {
+    const int nthr = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const T *src = (const T *)lut;
+    for (int t = tid; t < 4 * rows; t += nthr) {
+        const int r = t >> 2, c = t & 3;
+        dst[t] = (r < n && c < 3) ? src[3 * r + c] : T(0);
+    }
+}
+
+// One padded table row (three values) from shared memory.
+__device__ __forceinline__ void lut_row(float *m, const float *row) {
+    const float4 q = *reinterpret_cast<const float4 *>(row);
+    m[0] = q.x;
+    m[1] = q.y;
+    m[2] = q.z;
+}
+__device__ __forceinline__ void lut_row(double *m, const double *row) {
+    const double2 q = *reinterpret_cast<const double2 *>(row);
+    m[0] = q.x;
+    m[1] = q.y;
+    m[2] = row[2];
+}
+
+// The inverse material of a thread's V cells from the stage: the values
+// (MAT_FULL, at value offset oo of the material tile), the table rows of
+// their indices (MAT_IDS, at byte offset io), or the one table row.
+template <class T, int V, int MAT>
+__device__ __forceinline__ void stage_material(T (&m)[3 * V], const unsigned char *tile, int oo, int io,
+                                               const T *lut) {
+    if constexpr (MAT == MAT_FULL) {
+        ld_vec(m, reinterpret_cast<const T *>(tile) + oo);
+    } else if constexpr (MAT == MAT_IDS) {
+        unsigned char id[V];
+        if constexpr (V == 4) {
+            const uchar4 q = *reinterpret_cast<const uchar4 *>(tile + io);
+            id[0] = q.x;
+            id[1] = q.y;
+            id[2] = q.z;
+            id[3] = q.w;
+        } else {
+            const uchar2 q = *reinterpret_cast<const uchar2 *>(tile + io);
+            id[0] = q.x;
+            id[1] = q.y;
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) lut_row(m + 3 * v, lut + 4 * (int)id[v]);
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) lut_row(m + 3 * v, lut);
+    }
+}
+
+template <class P, int TZ, int TY, int MAT>
 __global__ void __launch_bounds__(TZ *TY)
     k_update_E_tma(const GridK g, const double *__restrict__ wave, const __grid_constant__ CUtensorMap tmN,
                    const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmM,
                    const __grid_constant__ CUtensorMap tmL) {
     using T = typename P::T;
-    using G = StageGeom<T, TZ, TY, P::COMP>;
+    using G = StageGeom<T, TZ, TY, P::COMP, MAT>;
     constexpr int V = G::V;
     constexpr int N = 3 * V;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -185,6 +246,8 @@ __global__ void __launch_bounds__(TZ *TY)
     const int SB = g.stage_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)S * SB);
     T *ctab = reinterpret_cast<T *>(smem + (size_t)S * SB + 8 * (size_t)S);
+    // material table (MAT_IDS, MAT_UNIFORM): padded rows, 16-byte aligned
+    T *mlut = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(ctab + g.coef_values) + 15) & ~uintptr_t(15));
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
@@ -213,12 +276,14 @@ __global__ void __launch_bounds__(TZ *TY)
         fence_proxy_async();
     }
     if (g.coef_values) stage_coef_tables<T>(g, ctab, true);
+    if constexpr (MAT != MAT_FULL) stage_material_table<T>(g.mlut_E, g.nlut_E, g.lut_rows, mlut);
     __syncthreads();
 
     auto issue = [&](int r) {
         const int p = xa + r;
         fill_stage<T, TY>(g, smem + (size_t)(r % S) * SB, smem_u32(&bars[r % S]), p, true, true, k0c, j0, G::Zc,
-                          &tmN, xN, p * ny + j0 - 1, &tmF, &tmM, &tmL, P::COMP, xO, G::ownOff, G::ownStride);
+                          &tmN, xN, p * ny + j0 - 1, &tmF, &tmM, &tmL, P::COMP, xO, k0c, MAT, G::txBytes, G::ownOff,
+                          G::matOff, G::loOff);
     };
     int issued = 0;
     for (; issued < min(S, np); ++issued)
@@ -239,16 +304,15 @@ __global__ void __launch_bounds__(TZ *TY)
         if (act && ok) {
             const T *Hn = reinterpret_cast<const T *>(st);
             const T *Ef = reinterpret_cast<const T *>(st + G::ownOff);
-            const T *Mf = reinterpret_cast<const T *>(st + G::ownOff + G::ownStride);
             const int on = (ty + 1) * G::pitchN + 4 + 3 * tz * V;  // own row in the neighbour tile
             const int oo = ty * G::pitchO + 3 * tz * V;
             alignas(16) T hc[N], hj[N], e[N], el[N], m[N];
             ld_vec(hc, Hn + on);
             ld_vec(hj, Hn + on - G::pitchN);
             ld_vec(e, Ef + oo);
-            ld_vec(m, Mf + oo);
+            stage_material<T, V, MAT>(m, st + G::matOff, oo, ty * G::Zc + tz * V, mlut);
             if constexpr (P::COMP) {
-                ld_vec(el, reinterpret_cast<const T *>(st + G::ownOff + 2 * G::ownStride) + oo);
+                ld_vec(el, reinterpret_cast<const T *>(st + G::loOff) + oo);
             } else {
 #pragma unroll
                 for (int q = 0; q < N; ++q) el[q] = T(0);
@@ -279,13 +343,13 @@ __global__ void __launch_bounds__(TZ *TY)
     }
 }
 
-template <class P, int TZ, int TY>
+template <class P, int TZ, int TY, int MAT>
 __global__ void __launch_bounds__(TZ *TY)
     k_update_H_tma(const GridK g, const double *__restrict__ wave, const __grid_constant__ CUtensorMap tmN,
                    const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmM,
                    const __grid_constant__ CUtensorMap tmL) {
     using T = typename P::T;
-    using G = StageGeom<T, TZ, TY, P::COMP>;
+    using G = StageGeom<T, TZ, TY, P::COMP, MAT>;
     constexpr int V = G::V;
     constexpr int N = 3 * V;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -295,6 +359,8 @@ __global__ void __launch_bounds__(TZ *TY)
     const int SB = g.stage_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (size_t)S * SB);
     T *ctab = reinterpret_cast<T *>(smem + (size_t)S * SB + 8 * (size_t)S);
+    // material table (MAT_IDS, MAT_UNIFORM): padded rows, 16-byte aligned
+    T *mlut = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(ctab + g.coef_values) + 15) & ~uintptr_t(15));
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
@@ -321,12 +387,14 @@ __global__ void __launch_bounds__(TZ *TY)
         fence_proxy_async();
     }
     if (g.coef_values) stage_coef_tables<T>(g, ctab, false);
+    if constexpr (MAT != MAT_FULL) stage_material_table<T>(g.mlut_H, g.nlut_H, g.lut_rows, mlut);
     __syncthreads();
 
     auto issue = [&](int r) {
         const int p = xa + r;
         fill_stage<T, TY>(g, smem + (size_t)(r % S) * SB, smem_u32(&bars[r % S]), p, p < xb, false, k0c, j0,
-                          G::Zc, &tmN, xO, p * ny + j0, &tmF, &tmM, &tmL, P::COMP, xO, G::ownOff, G::ownStride);
+                          G::Zc, &tmN, xO, p * ny + j0, &tmF, &tmM, &tmL, P::COMP, xO, k0c, MAT, G::txBytes,
+                          G::ownOff, G::matOff, G::loOff);
     };
     int issued = 0;
     for (; issued < min(S, nfill); ++issued)
@@ -345,7 +413,6 @@ __global__ void __launch_bounds__(TZ *TY)
             const T *En = reinterpret_cast<const T *>(st);
             const T *Ex1 = reinterpret_cast<const T *>(sn);
             const T *Hf = reinterpret_cast<const T *>(st + G::ownOff);
-            const T *Mf = reinterpret_cast<const T *>(st + G::ownOff + G::ownStride);
             const int on = ty * G::pitchN + 3 * tz * V;
             const int oo = ty * G::pitchO + 3 * tz * V;
             alignas(16) T ec[N], en[N], ej[N], h[N], hl[N], m[N];
@@ -353,9 +420,9 @@ __global__ void __launch_bounds__(TZ *TY)
             ld_vec(ej, En + on + G::pitchN);
             ld_vec(en, Ex1 + on);
             ld_vec(h, Hf + oo);
-            ld_vec(m, Mf + oo);
+            stage_material<T, V, MAT>(m, st + G::matOff, oo, ty * G::Zc + tz * V, mlut);
             if constexpr (P::COMP) {
-                ld_vec(hl, reinterpret_cast<const T *>(st + G::ownOff + 2 * G::ownStride) + oo);
+                ld_vec(hl, reinterpret_cast<const T *>(st + G::loOff) + oo);
             } else {
 #pragma unroll
                 for (int q = 0; q < N; ++q) hl[q] = T(0);

@@ -37,6 +37,63 @@ def _require_gpu(grid):
     return _native.load()
 
 
+_MAX_TABLE = 256  # distinct value triples a one-byte material index can address
+
+
+def compact_material(x, chunk=1 << 25, index_ok=True):
+    """Compact copy of a (nx, ny, nz, 3) inverse-material array for the staged
+    passes: ``(table, index)`` with ``table`` the (n, 3) distinct value triples
+    and ``index`` the uint8 (nx, ny, nz) row of every cell, or ``(table, None)``
+    when every cell holds the same triple; ``None`` when there are more than 256
+    triples, or more than one and ``index_ok`` is false.  Values are compared as bit patterns, so signed zeros and NaN
+    payloads keep their table rows and ``table[index] == x`` holds bit for bit."""
+    itype = torch.int32 if x.element_size() == 4 else torch.int64
+    bits = x.contiguous().view(itype).reshape(-1, 3)
+    ncell = bits.shape[0]
+    if ncell == 0:
+        return None
+    # quick rejection on a strided sample (random media, graded profiles)
+    step = max(1, ncell // 65536)
+    if torch.unique(bits[::step], dim=0).shape[0] > _MAX_TABLE:
+        return None
+    # distinct values per component
+    comps = []
+    for c in range(3):
+        parts = [torch.unique(bits[a:a + chunk, c]) for a in range(0, ncell, chunk)]
+        u = torch.unique(torch.cat(parts)) if len(parts) > 1 else parts[0]
+        if u.numel() > _MAX_TABLE:
+            return None
+        comps.append(u)
+    n0, n1, n2 = (u.numel() for u in comps)
+    if n0 == n1 == n2 == 1:
+        return x.reshape(-1, 3)[:1].clone(), None
+    if not index_ok:
+        return None
+
+    def keys(a):
+        blk = bits[a:a + chunk]
+        k = torch.searchsorted(comps[0], blk[:, 0].contiguous())
+        k = k * n1 + torch.searchsorted(comps[1], blk[:, 1].contiguous())
+        return k * n2 + torch.searchsorted(comps[2], blk[:, 2].contiguous())
+
+    present = torch.zeros(n0 * n1 * n2, dtype=torch.bool, device=x.device)
+    for a in range(0, ncell, chunk):
+        present[keys(a)] = True
+    rows = torch.nonzero(present).reshape(-1)
+    if rows.numel() > _MAX_TABLE:
+        return None
+    rank = torch.zeros(n0 * n1 * n2, dtype=torch.uint8, device=x.device)
+    rank[rows] = torch.arange(rows.numel(), device=x.device).to(torch.uint8)
+    index = torch.empty(ncell, dtype=torch.uint8, device=x.device)
+    for a in range(0, ncell, chunk):
+        index[a:a + chunk] = rank[keys(a)]
+    i2 = rows % n2
+    i1 = (rows // n2) % n1
+    i0 = rows // (n1 * n2)
+    table = torch.stack([comps[0][i0], comps[1][i1], comps[2][i2]], dim=1).view(x.dtype).contiguous()
+    return table, index.reshape(x.shape[:-1])
+
+
 class _PinnedStager:
     """Double-buffered pinned host staging for small per-call tables."""
 
@@ -69,12 +126,15 @@ class Engine:
         self.grid = grid
         self.x_chunk = x_chunk
         # fused-pass kernel choice: variant 0 auto / 1 register streaming / 2 TMA-staged
-        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0}
+        # materials: 0 compact copies for the staged passes where possible, 1 full arrays only
+        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0, "materials": 0}
         self.plan = None
         self._key = None
         self._keep = []
         self._scaled = None
         self._scaled_keys = [None, None]
+        self._compact = [None, None]  # per material: (table, index or None) or None
+        self._compact_keys = [None, None]
         self.trace_E = self.trace_H = self.trace_I = None
         self.capacity = 0
         self.rec_E = self.rec_H = self.rec_I = 0
@@ -100,7 +160,8 @@ class Engine:
         key = self._state_key()
         if self.plan is not None and not g._dirty and key == self._key:
             self._sync_scaled_materials()
-            return
+            if not self._sync_compact_materials():
+                return
         self._build()
         self._key = self._state_key()
         g._dirty = False
@@ -119,17 +180,65 @@ class Engine:
                 torch.mul(src, g.courant_number, out=dst)
                 self._scaled_keys[ver] = key
 
+    def _material_arrays(self):
+        g = self.grid
+        if self._scaled is not None:
+            return self._scaled
+        return g._inverse_permittivity, g._inverse_permeability
+
+    @staticmethod
+    def _layout(enc):
+        if enc is None:
+            return None
+        return (enc[0].shape[0], enc[1] is not None)
+
+    # compact copies follow in-place changes of the material arrays; returns
+    # True when their layout changed and the plan must be rebuilt
+    def _sync_compact_materials(self):
+        g = self.grid
+        want = self.tuning["materials"] == 0
+        rebuild = False
+        for q, src in enumerate(self._material_arrays()):
+            key = (src.data_ptr(), src._version, want)
+            if self._compact_keys[q] == key:
+                continue
+            # index maps are read by TMA in rows of nz bytes: nz a multiple of 16
+            enc = compact_material(src, index_ok=g.Nz % 16 == 0) if want else None
+            old = self._compact[q]
+            if enc is not None and old is not None and self._layout(enc) == self._layout(old):
+                old[0].copy_(enc[0])
+                if enc[1] is not None:
+                    old[1].copy_(enc[1])
+            else:
+                rebuild |= self._layout(enc) != self._layout(old)
+                self._compact[q] = enc
+            self._compact_keys[q] = key
+        return rebuild
+
+    def compact_materials(self):
+        """How the plan's staged passes read each material (inverse permittivity,
+        inverse permeability): None (full arrays; always for the register
+        kernels), ("uniform", 1) or ("index", n distinct value triples)."""
+        if self.plan is None or self.tiling()["variant"] != 2:
+            return [None, None]
+        return [None if e is None else (("index", e[0].shape[0]) if e[1] is not None else ("uniform", 1))
+                for e in self._compact]
+
     def set_x_chunk(self, x_chunk):
         self.x_chunk = int(x_chunk)
         self.refresh()
 
-    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None):
+    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None, materials=None):
         """Choose the fused-pass kernels (0 auto, 1 register streaming, 2 TMA-staged),
         the TMA tile rows (4 or 8 with 32-thread-wide tiles, 16 with 16-wide) and
-        ring stages, and where the PML slabs run
-        (0 auto, 1 inside the fused pass, 2 kernels of their own); 0 keeps the
-        automatic choice."""
-        for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode)):
+        ring stages, where the PML slabs run
+        (0 auto, 1 inside the fused pass, 2 kernels of their own; 3 only the
+        leading x/y slabs split off), and how the staged passes read the
+        materials (0 a one-byte index into a table of distinct value triples,
+        or nothing for a uniform material, where the materials allow; 1 the
+        full arrays); 0 keeps the automatic choice."""
+        for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode),
+                     ("materials", materials)):
             if v is not None:
                 self.tuning[k] = int(v)
         if x_chunk is not None:
@@ -212,8 +321,18 @@ class Engine:
             d.inv_eps, d.inv_mu = self._scaled[0].data_ptr(), self._scaled[1].data_ptr()
             d.materials_scaled = 1
         else:
+            self._scaled = None
             d.inv_eps = g._inverse_permittivity.data_ptr()
             d.inv_mu = g._inverse_permeability.data_ptr()
+        self._compact_keys = [None, None]
+        self._compact = [None, None]
+        self._sync_compact_materials()
+        for enc, tab, n, idx in ((self._compact[0], "eps_table", "n_eps_table", "eps_index"),
+                                 (self._compact[1], "mu_table", "n_mu_table", "mu_index")):
+            if enc is not None:
+                setattr(d, tab, enc[0].data_ptr())
+                setattr(d, n, enc[0].shape[0])
+                setattr(d, idx, enc[1].data_ptr() if enc[1] is not None else None)
 
         if len(g.boundaries) > _native.MAX_BOUNDARIES:
             raise NotImplementedError("more boundaries than the gb300 backend supports")

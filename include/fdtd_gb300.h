@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 3
+#define FDTD_ABI_VERSION 4
 #define FDTD_MAX_BOUNDARIES 9 /* six PML slabs and three periodic axes */
 
 typedef void *fdtd_stream_t; /* a cudaStream_t */
@@ -169,6 +169,20 @@ typedef struct {
                                          courant * inverse_permittivity / permeability (the
                                          products the reference forms first), so the kernels
                                          skip that multiply; 0 = plain inverse materials */
+    /* Optional compact copies of inv_eps / inv_mu for the TMA-staged passes
+     * (inv_eps and inv_mu stay required in full for the other kernels): a
+     * table of n value triples (plan element type) and a one-byte index per
+     * cell ([nx][ny][nz], nz a multiple of 16) with inv_eps[cell] ==
+     * table[index[cell]] for every cell; or n = 1 and index = NULL when every
+     * cell holds table[0].  The staged passes then read one byte per cell, or
+     * nothing, instead of three values.  n = 0: not given.  The caller keeps
+     * the copies consistent with the full arrays. */
+    const void *eps_table;
+    int32_t n_eps_table;                /* 0 .. 256 */
+    const uint8_t *eps_index;
+    const void *mu_table;
+    int32_t n_mu_table;
+    const uint8_t *mu_index;
 } fdtd_grid_desc;
 
 typedef struct fdtd_plan fdtd_plan;

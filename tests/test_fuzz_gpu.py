@@ -1,10 +1,12 @@
 """Seeded random scenes: the CUDA time step against the CPU oracle.
 
-Every scene draws a grid shape (odd and even nz, sometimes 2D), PML slabs and
+Every scene draws a grid shape (odd and even nz, sometimes 2D), a random or a
+few-valued permittivity (the latter read through compact material copies by
+the staged passes), PML slabs and
 periodic boundaries on random axes in a random registration order, up to
 three overlapping objects of all kinds, point, line and plane sources,
 line/block/plane detectors, and a plan choice (kernel variant, PML mode, tile
-rows, x chunk).  float64 must match the oracle to 1e-12 relative L2, float32
+rows, x chunk, material copies).  float64 must match the oracle to 1e-12 relative L2, float32
 to 1e-4, on E, H and every detector trace.
 """
 
@@ -19,9 +21,14 @@ pytestmark = pytest.mark.gpu
 
 def random_scene(mod, seed):
     rng = np.random.default_rng(seed)
+    side = np.random.default_rng(seed + 2000)  # draws added later, kept off the main stream
     nz = int(rng.choice([1, 7, 8, 12, 13, 16]))
+    if nz == 16 and side.random() < 0.5:
+        nz = 32
     nx, ny = int(rng.integers(8, 19)), int(rng.integers(8, 19))
     eps = rng.uniform(1.0, 3.0, size=(nx, ny, nz))
+    if side.random() < 0.5:
+        eps = np.round(eps * 2.0) / 2.0  # a few distinct values: compact material copies
     grid = mod.Grid((nx, ny, nz), grid_spacing=120e-9, permittivity=eps)
     n = (nx, ny, nz)
     # boundaries: per axis none / PML on one or both sides / periodic
@@ -88,7 +95,8 @@ def random_scene(mod, seed):
 def random_tuning(seed, nz, precision):
     rng = np.random.default_rng(seed + 1000)
     vmax = 2 if precision == "float64" else 4
-    tune = {"pml_mode": int(rng.integers(0, 4)), "x_chunk": int(rng.choice([0, 3, 5]))}
+    tune = {"pml_mode": int(rng.integers(0, 4)), "x_chunk": int(rng.choice([0, 3, 5])),
+            "materials": int(np.random.default_rng(seed + 3000).integers(0, 2))}
     if nz % vmax == 0 and rng.random() < 0.5:
         tune.update(variant=2, tile_rows=int(rng.choice([4, 8, 16])), stages=int(rng.choice([2, 3])))
     else:
@@ -111,7 +119,7 @@ def test_random_scene_matches_oracle(fd, seed, precision):
         eng.set_tuning(**tune)
     except RuntimeError:
         # a staged tile that the slab count or shared memory does not allow
-        tune = {"variant": 1, "pml_mode": tune["pml_mode"]}
+        tune = {"variant": 1, "pml_mode": tune["pml_mode"], "materials": tune["materials"]}
         eng.set_tuning(variant=1, tile_rows=0, stages=0)
     steps = 15
     g.run(steps, progress_bar=False)

@@ -1,0 +1,149 @@
+"""Compact material copies on the GPU.
+
+The staged passes can read a one-byte index per cell into a shared-memory
+table of the distinct inverse-material triples, or nothing when the material
+is uniform, instead of three values per cell.  The values and the arithmetic
+are unchanged, so E, H and every detector trace must be bit-identical to the
+same plan reading the full arrays, and match the oracle (float64 1e-12,
+float32 1e-4 relative L2).  In-place changes of the materials between runs
+must be followed.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import rel_l2
+from oracle import fdtd_oracle as fo
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"float64": 1e-12, "float32": 1e-4, "float32c": 1e-4}
+
+
+def scene(mod, nz=32, levels=True, objects=True, pml=True):
+    nx, ny = 20, 18
+    rng = np.random.default_rng(7)
+    eps = rng.choice([1.0, 1.5, 2.25, 3.0], size=(nx, ny, nz)) if levels else 1.0
+    grid = mod.Grid((nx, ny, nz), grid_spacing=100e-9, permittivity=eps, permeability=1.0)
+    if pml:
+        grid[0:3, :, :] = mod.PML(name="pxlo")
+        grid[-3:, :, :] = mod.PML(name="pxhi")
+        grid[:, :, -4:] = mod.PML(name="pzhi")
+    grid[:, 0, :] = mod.PeriodicBoundary(name="py")
+    if objects:
+        grid[5:9, 4:10, 6:14] = mod.Object(permittivity=2.0, name="obj")
+        grid[11:14, 9:13, 12:20] = mod.AbsorbingObject(permittivity=1.5, conductivity=2e4, name="absorber")
+        grid[7:10, 12:16, 18:24] = mod.AnisotropicObject(permittivity=2.5, name="aniso")
+    grid[10, 9, 16] = mod.PointSource(period=14, name="src")
+    grid[:, :, 9] = mod.PlaneSource(period=18, amplitude=0.5, polarization="x", name="plane")
+    grid[4:16, 9, 16] = mod.LineDetector(name="line")
+    grid[8:10, 8:10, 20:22] = mod.BlockDetector(name="block")
+    return grid
+
+
+def _records(grid):
+    out = [grid.E, grid.H]
+    for d in grid.detectors:
+        out += [torch.as_tensor(np.asarray(d.E)), torch.as_tensor(np.asarray(d.H))]
+    return [torch.as_tensor(t).detach().cpu() for t in out]
+
+
+def _bits(t):
+    return t.view(torch.int32 if t.dtype == torch.float32 else torch.int64)
+
+
+def _run(fd, precision, tune, materials, steps=20, **kw):
+    fd.set_backend("gb300." + precision)
+    g = scene(fd, **kw)
+    eng = g._ensure_engine()
+    eng.set_tuning(variant=2, materials=materials, **tune)
+    g.run(steps, progress_bar=False)
+    eng.check_status()
+    return g, eng
+
+
+TUNES = [dict(tile_rows=8, pml_mode=1), dict(tile_rows=4, pml_mode=2), dict(tile_rows=16, pml_mode=2),
+         dict(tile_rows=8, pml_mode=2, stages=2)]
+
+
+@pytest.mark.parametrize("tune", TUNES, ids=lambda t: "-".join(f"{k}{v}" for k, v in t.items()))
+@pytest.mark.parametrize("precision", ["float64", "float32", "float32c"])
+def test_index_materials_bit_identical_to_full(fd, precision, tune):
+    g, eng = _run(fd, precision, tune, materials=0)
+    modes = eng.compact_materials()
+    assert modes[0][0] == "index" and modes[1] == ("uniform", 1), modes
+    assert eng.tiling()["variant"] == 2
+    f, feng = _run(fd, precision, tune, materials=1)
+    assert feng.compact_materials() == [None, None]
+    for a, b in zip(_records(g), _records(f)):
+        assert torch.equal(_bits(a), _bits(b))
+    o = scene(fo)
+    o.run(20)
+    assert rel_l2(g.E, o.E) <= TOL[precision] and rel_l2(g.H, o.H) <= TOL[precision]
+    for d, od in zip(g.detectors, o.detectors):
+        assert rel_l2(np.asarray(d.E), np.stack(od.E)) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_uniform_materials(fd, precision):
+    kw = dict(levels=False, objects=False)
+    g, eng = _run(fd, precision, dict(tile_rows=8), materials=0, **kw)
+    assert eng.compact_materials() == [("uniform", 1), ("uniform", 1)]
+    f, _ = _run(fd, precision, dict(tile_rows=8), materials=1, **kw)
+    for a, b in zip(_records(g), _records(f)):
+        assert torch.equal(_bits(a), _bits(b))
+
+
+def test_random_medium_falls_back_to_full_arrays(fd):
+    fd.set_backend("gb300.float32")
+    g = fd.Grid((16, 16, 32), grid_spacing=100e-9,
+                permittivity=np.random.default_rng(1).uniform(1.0, 3.0, size=(16, 16, 32)))
+    g[8, 8, 16] = fd.PointSource(period=12)
+    eng = g._ensure_engine()
+    eng.set_tuning(variant=2)
+    assert eng.compact_materials()[0] is None and eng.compact_materials()[1] == ("uniform", 1)
+    g.run(5, progress_bar=False)
+    eng.check_status()
+
+
+def test_index_needs_nz_multiple_of_16(fd):
+    fd.set_backend("gb300.float32")
+    g = scene(fd, nz=24)
+    eng = g._ensure_engine()
+    eng.set_tuning(variant=2, tile_rows=8)
+    assert eng.compact_materials() == [None, ("uniform", 1)]
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_in_place_material_changes_are_followed(fd, precision):
+    fd.set_backend("gb300." + precision)
+    g = scene(fd)
+    o = scene(fo)
+    eng = g._ensure_engine()
+    eng.set_tuning(variant=2, tile_rows=8, pml_mode=2)
+    g.run(8, progress_bar=False)
+    o.run(8)
+    n0 = eng.compact_materials()[0][1]
+    # an existing value triple: same table size, updated in place
+    g.inverse_permittivity[14:18, 2:6, 2:30] = 1.0 / 1.5
+    o.inverse_permittivity[14:18, 2:6, 2:30] = 1.0 / 1.5
+    g.run(8, progress_bar=False)
+    o.run(8)
+    assert eng.compact_materials()[0][1] == n0
+    # a new value triple: larger table, plan rebuilt
+    g.inverse_permittivity[2:5, 3:7, 1:5] = 0.3
+    o.inverse_permittivity[2:5, 3:7, 1:5] = 0.3
+    g.run(8, progress_bar=False)
+    o.run(8)
+    assert eng.compact_materials()[0][1] == n0 + 1
+    # a uniform permeability that stops being uniform
+    g.inverse_permeability[6:8, 6:8, 6:8] = 0.5
+    o.inverse_permeability[6:8, 6:8, 6:8] = 0.5
+    g.run(8, progress_bar=False)
+    o.run(8)
+    assert eng.compact_materials()[1] == ("index", 2)
+    eng.check_status()
+    assert rel_l2(g.E, o.E) <= TOL[precision] and rel_l2(g.H, o.H) <= TOL[precision]
+    for d, od in zip(g.detectors, o.detectors):
+        assert rel_l2(np.asarray(d.E), np.stack(od.E)) <= TOL[precision]
