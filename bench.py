@@ -191,14 +191,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile(precision, n):
-    """DRAM bytes per fused-kernel launch from the committed ncu summary, if any."""
+def traffic_from_profile(precision, n, half, materials):
+    """DRAM bytes of one half step (fused pass and its slab kernels) from the
+    committed ncu summary, if it covers this precision and material layout."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
-    if not os.path.exists(path):
+    if not os.path.exists(path) or materials != {"E": ["index", 3], "H": ["uniform", 1]}:
         return None
     with open(path) as f:
         d = json.load(f)
-    ent = d.get(precision)
+    ent = d.get(precision, {}).get(half)
     if not ent:
         return None
     # per-cell traffic measured on a smaller grid, scaled to this workload
@@ -444,7 +445,7 @@ def gb300_arm(args):
     t_kern = main["half_ms"][kern] if "half_ms" in main else main["ms_per_step"] / 2
     algo_kern = main["algo_bytes"][kern]
     achieved = algo_kern / (t_kern * 1e-3) / 1e9
-    traffic = traffic_from_profile(precs[0], n)
+    traffic = traffic_from_profile(precs[0], n, kern, json.loads(json.dumps(main["materials"])))
     line = {
         "metric": METRIC,
         "value": main["gcells"],

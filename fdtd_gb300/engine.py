@@ -45,30 +45,44 @@ def compact_material(x, chunk=1 << 25, index_ok=True):
     passes: ``(table, index)`` with ``table`` the (n, 3) distinct value triples
     and ``index`` the uint8 (nx, ny, nz) row of every cell, or ``(table, None)``
     when every cell holds the same triple; ``None`` when there are more than 256
-    triples, or more than one and ``index_ok`` is false.  Values are compared as bit patterns, so signed zeros and NaN
-    payloads keep their table rows and ``table[index] == x`` holds bit for bit."""
+    triples, or more than one and ``index_ok`` is false.  Values are compared as
+    bit patterns, so signed zeros and NaN payloads keep their table rows and
+    ``table[index] == x`` holds bit for bit.  One pass decides uniformity; the
+    distinct values of each component come from a strided sample, checked
+    against every cell by binary search (a sort of the missing values only
+    when the sample missed some)."""
     itype = torch.int32 if x.element_size() == 4 else torch.int64
     bits = x.contiguous().view(itype).reshape(-1, 3)
     ncell = bits.shape[0]
     if ncell == 0:
         return None
-    # quick rejection on a strided sample (random media, graded profiles)
-    step = max(1, ncell // 65536)
-    if torch.unique(bits[::step], dim=0).shape[0] > _MAX_TABLE:
+    first = bits[:1]
+    if all(bool((bits[a:a + chunk] == first).all()) for a in range(0, ncell, chunk)):
+        return x.reshape(-1, 3)[:1].clone(), None
+    if not index_ok:
         return None
-    # distinct values per component
+    # quick rejection on a strided sample (random media, graded profiles)
+    sample = bits[::max(1, ncell // 65536)]
+    if torch.unique(sample, dim=0).shape[0] > _MAX_TABLE:
+        return None
     comps = []
     for c in range(3):
-        parts = [torch.unique(bits[a:a + chunk, c]) for a in range(0, ncell, chunk)]
-        u = torch.unique(torch.cat(parts)) if len(parts) > 1 else parts[0]
+        u = torch.unique(sample[:, c])
+        missing = []
+        for a in range(0, ncell, chunk):
+            col = bits[a:a + chunk, c].contiguous()
+            pos = torch.searchsorted(u, col).clamp_(max=u.numel() - 1)
+            bad = u[pos] != col
+            if bool(bad.any()):
+                missing.append(torch.unique(col[bad]))
+                if sum(m.numel() for m in missing) > _MAX_TABLE:
+                    return None
+        if missing:
+            u = torch.unique(torch.cat([u] + missing))
         if u.numel() > _MAX_TABLE:
             return None
         comps.append(u)
     n0, n1, n2 = (u.numel() for u in comps)
-    if n0 == n1 == n2 == 1:
-        return x.reshape(-1, 3)[:1].clone(), None
-    if not index_ok:
-        return None
 
     def keys(a):
         blk = bits[a:a + chunk]

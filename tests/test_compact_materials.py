@@ -73,3 +73,15 @@ def test_index_not_allowed():
     assert compact_material(x, index_ok=False)[1] is None
     x[0, 0, 0, 0] = 1.0
     assert compact_material(x, index_ok=False) is None
+
+
+def test_values_the_sample_misses():
+    """A value present in only a few cells (missed by the strided sample)
+    still gets its own table row."""
+    x = torch.full((64, 64, 32, 3), 0.5, dtype=torch.float32)
+    x[::2] = 0.25
+    x[17, 33, 5, 1] = 0.125
+    x[63, 63, 31, 2] = -0.0
+    table, index = compact_material(x, chunk=5000)
+    assert torch.equal(table[index.long()].view(torch.int32), x.view(torch.int32))
+    assert table.shape[0] == 4
