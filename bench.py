@@ -191,11 +191,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile(precision, n, half, materials):
+def traffic_from_profile(precision, n, half, materials, automatic_plan):
     """DRAM bytes of one half step (fused pass and its slab kernels) from the
-    committed ncu summary, if it covers this precision and material layout."""
+    committed ncu summary, if it covers this precision, material layout and
+    (automatic) plan."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
-    if not os.path.exists(path) or materials != {"E": ["index", 3], "H": ["uniform", 1]}:
+    if (not os.path.exists(path) or not automatic_plan
+            or materials != {"E": ["index", 3], "H": ["uniform", 1]}):
         return None
     with open(path) as f:
         d = json.load(f)
@@ -445,7 +447,8 @@ def gb300_arm(args):
     t_kern = main["half_ms"][kern] if "half_ms" in main else main["ms_per_step"] / 2
     algo_kern = main["algo_bytes"][kern]
     achieved = algo_kern / (t_kern * 1e-3) / 1e9
-    traffic = traffic_from_profile(precs[0], n, kern, json.loads(json.dumps(main["materials"])))
+    automatic = (args.variant, args.tile_rows, args.stages, args.pml_mode, args.materials, args.x_chunk) == (0,) * 6
+    traffic = traffic_from_profile(precs[0], n, kern, json.loads(json.dumps(main["materials"])), automatic)
     line = {
         "metric": METRIC,
         "value": main["gcells"],

@@ -237,19 +237,26 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     //
     // Mode 3 keeps the slabs normal to x or y that lead the boundary list
     // inside the fused pass (their extra work is the same for every warp of a
-    // CTA) and splits off the rest.  Measured slower than splitting every slab
-    // (config 3: 58.0 vs 63.2 Gcell/s, config 5: 25.5 vs 32.3): the staged
-    // auxiliary rows shrink the shared-memory ring from 6 to 4 stages and the
-    // in-pass slab path costs more than the slab kernels' re-reads, so the
-    // automatic choice splits every slab.
+    // CTA) and splits off the rest.  With full material arrays and one CTA per
+    // SM it measured slower than splitting every slab (config 3: 58.0 vs 63.2
+    // Gcell/s).  With compact material copies and two CTAs per SM it is the
+    // faster float32 plan on config 3 (80.8 vs 78.7 Gcell/s) but not the
+    // faster float64 (15.1 vs 15.3) or float32c (47.0 vs 48.2) plan, whose
+    // fused passes are arithmetic-bound, and keeping leading x slabs as well
+    // slowed config 5 (x, y, z slab pairs) by 29%: whole slab planes make the
+    // CTAs that hold them late, and their auxiliary rows enlarge every stage.
+    // The automatic choice therefore keeps only leading y slabs, for float32
+    // with compact materials.
     const long ncell = (long)d->nx * d->ny * d->nz;
     p.pml_split = g.nslab > 0 &&
                   (d->pml_mode >= 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768 &&
                                         ncell >= (8L << 20)));
     int kfs = 0;  // leading slabs kept in the fused pass when split
-    if (p.pml_split && d->pml_mode == 3) {
+    const bool auto_keep = d->pml_mode == 0 && d->precision == FDTD_FLOAT32 && mat_want[0] != MAT_FULL &&
+                           mat_want[1] != MAT_FULL;
+    if (p.pml_split && (d->pml_mode == 3 || auto_keep)) {
         while (kfs < d->n_boundaries && d->boundaries[kfs].kind == FDTD_BOUNDARY_PML &&
-               d->boundaries[kfs].axis != 2)
+               (auto_keep ? d->boundaries[kfs].axis == 1 : d->boundaries[kfs].axis != 2))
             ++kfs;
         if (kfs == g.nslab) {  // nothing left to split off
             p.pml_split = 0;
@@ -408,6 +415,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             g.lut_rows = lut_rows;
             p.index_E = d->eps_index;
             p.index_H = d->mu_index;
+            g.mid_E = g.mat_E == MAT_IDS ? d->eps_index : nullptr;
+            g.mid_H = g.mat_H == MAT_IDS ? d->mu_index : nullptr;
         }
     }
     if (!use_tma) {

@@ -74,6 +74,7 @@ struct GridK {
     const void *mlut_E, *mlut_H;
     int nlut_E, nlut_H;
     int lut_rows;  // padded 4-value rows reserved for the table in shared memory
+    const unsigned char *mid_E, *mid_H;  // one-byte material indices (MAT_IDS)
 };
 
 template <class T>

@@ -235,32 +235,57 @@ __global__ void k_slab_correct(const GridK g, int s) {
 // update of fdtd/boundaries.py:433-487 with the slab-local index rules, then
 // the correction of fdtd/boundaries.py:409-431, per slab cell and with the
 // same per-cell arithmetic as the fused pass.  The neighbour field is not
-// written during the half step, so its differences can be read here.
-template <class P, bool IS_E>
+// written during the half step, so its differences can be read here.  The
+// slab normal A is a template parameter and the cell index type I is 32-bit
+// whenever the slab has fewer than 2^31 cells (no 64-bit divisions); all
+// buffers are distinct, so every load of a cell can issue up front.
+template <class P, bool IS_E, int A, class I>
 __global__ void __launch_bounds__(kThreads) k_pml_slab(const GridK g, int s) {
     using T = typename P::T;
     const SlabK &S = g.slab[s];
-    const int a = S.axis;
-    const int n0 = a == 0 ? S.th : g.nx, n1 = a == 1 ? S.th : g.ny, n2 = a == 2 ? S.th : g.nz;
-    const int p2 = a == 2 ? S.thp : g.nz;
-    const long total = (long)n0 * n1 * n2;
+    const int n1 = A == 1 ? S.th : g.ny, n2 = A == 2 ? S.th : g.nz;
+    const int p2 = A == 2 ? S.thp : g.nz;
+    const I total = (I)(A == 0 ? S.th : g.nx) * (I)n1 * (I)n2;
     const T c = courant_of<T>(g);
-    T *F = (T *)(IS_E ? g.E : g.H);
-    T *Flo = (T *)(IS_E ? g.Elo : g.Hlo);
+    T *__restrict__ F = (T *)(IS_E ? g.E : g.H);
+    T *__restrict__ Flo = (T *)(IS_E ? g.Elo : g.Hlo);
     const T *__restrict__ N = (const T *)(IS_E ? g.H : g.E);  // neighbour field
     const T *__restrict__ M = (const T *)(IS_E ? g.ie : g.imu);
-    T *psi = (T *)(IS_E ? S.psiE : S.psiH);
+    T *__restrict__ psi = (T *)(IS_E ? S.psiE : S.psiH);
     const T *__restrict__ bt = (const T *)(IS_E ? S.bE : S.bH);
     const T *__restrict__ ct = (const T *)(IS_E ? S.cE : S.cH);
-    const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
-    const long stride = a == 0 ? 3L * g.ny * g.nz : (a == 1 ? 3L * g.nz : 3L);
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const int i0 = (int)(t / ((long)n1 * n2)), i1 = (int)((t / n2) % n1), i2 = (int)(t % n2);
-        const int l = a == 0 ? i0 : (a == 1 ? i1 : i2);
-        const int gi = a == 0 ? i0 + S.start : i0, gj = a == 1 ? i1 + S.start : i1, gk = a == 2 ? i2 + S.start : i2;
-        const size_t at = 3 * (((size_t)gi * g.ny + gj) * g.nz + gk);
+    // materials: through the staged passes' compact copy when the plan has one
+    const int mat = IS_E ? g.mat_E : g.mat_H;
+    const T *__restrict__ lut = (const T *)(IS_E ? g.mlut_E : g.mlut_H);
+    const unsigned char *__restrict__ mid = IS_E ? g.mid_E : g.mid_H;
+    const int nlut = IS_E ? g.nlut_E : g.nlut_H;
+    constexpr int t1 = (A + 1) % 3, t2 = (A + 2) % 3;
+    const size_t stride = A == 0 ? 3 * (size_t)g.ny * g.nz : (A == 1 ? 3 * (size_t)g.nz : 3);
+    for (I t = (I)blockIdx.x * (I)blockDim.x + threadIdx.x; t < total; t += (I)gridDim.x * (I)blockDim.x) {
+        const I r = t / (I)n2;
+        const int i2 = (int)(t - r * (I)n2), i1 = (int)(r % (I)n1), i0 = (int)(r / (I)n1);
+        const int l = A == 0 ? i0 : (A == 1 ? i1 : i2);
+        const int gi = A == 0 ? i0 + S.start : i0, gj = A == 1 ? i1 + S.start : i1, gk = A == 2 ? i2 + S.start : i2;
+        const size_t cell = ((size_t)gi * g.ny + gj) * g.nz + gk;
+        const size_t at = 3 * cell;
         const size_t pt = 2 * (((size_t)i0 * n1 + i1) * p2 + i2);
         T p0 = psi[pt], p1 = psi[pt + 1];
+        T x1 = F[at + t1], x2 = F[at + t2];
+        T m1, m2;
+        if (mat == MAT_FULL) {
+            m1 = M[at + t1];
+            m2 = M[at + t2];
+        } else {
+            // a table row; an index past the table reads zeros, as in the staged passes
+            const int id = mat == MAT_IDS ? (int)mid[cell] : 0;
+            m1 = id < nlut ? lut[3 * id + t1] : T(0);
+            m2 = id < nlut ? lut[3 * id + t2] : T(0);
+        }
+        T l1 = T(0), l2 = T(0);
+        if constexpr (P::COMP) {
+            l1 = Flo[at + t1];
+            l2 = Flo[at + t2];
+        }
         const T b = bt[l], cc = ct[l];
         if (IS_E ? (l >= 1) : (l <= S.th - 2)) {
             // E: backward difference of H along the normal; H: forward difference of E
@@ -274,14 +299,8 @@ __global__ void __launch_bounds__(kThreads) k_pml_slab(const GridK g, int s) {
         }
         psi[pt] = p0;
         psi[pt + 1] = p1;
-        T x1 = F[at + t1], x2 = F[at + t2];
-        T l1 = T(0), l2 = T(0);
-        if constexpr (P::COMP) {
-            l1 = Flo[at + t1];
-            l2 = Flo[at + t2];
-        }
-        pml_correct<P, IS_E>(x1, l1, P::cm(c, M[at + t1]), -p0);
-        pml_correct<P, IS_E>(x2, l2, P::cm(c, M[at + t2]), p1);
+        pml_correct<P, IS_E>(x1, l1, P::cm(c, m1), -p0);
+        pml_correct<P, IS_E>(x2, l2, P::cm(c, m2), p1);
         P::finish(x1, l1);
         P::finish(x2, l2);
         F[at + t1] = x1;

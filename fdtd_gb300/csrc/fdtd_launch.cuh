@@ -20,6 +20,27 @@ static int check_launch() {
     return FDTD_OK;
 }
 
+// One slab kernel: one thread per cell with 32-bit cell indices below 2^31
+// cells, else a grid-stride loop with 64-bit indices.
+template <class P, bool IS_E, int A>
+static void launch_pml_slab_axis(const GridK &g, int slab, long cells, cudaStream_t st) {
+    if (cells < (1L << 31)) {
+        const unsigned blocks = (unsigned)((cells + kThreads - 1) / kThreads);
+        k_pml_slab<P, IS_E, A, uint32_t><<<blocks > 0 ? blocks : 1, kThreads, 0, st>>>(g, slab);
+    } else {
+        k_pml_slab<P, IS_E, A, uint64_t><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, slab);
+    }
+}
+
+template <class P, bool IS_E>
+static void launch_pml_slab(const GridK &g, int slab, cudaStream_t st) {
+    const SlabK &S = g.slab[slab];
+    const long cells = (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) * (S.axis == 2 ? S.th : g.nz);
+    if (S.axis == 0) launch_pml_slab_axis<P, IS_E, 0>(g, slab, cells, st);
+    else if (S.axis == 1) launch_pml_slab_axis<P, IS_E, 1>(g, slab, cells, st);
+    else launch_pml_slab_axis<P, IS_E, 2>(g, slab, cells, st);
+}
+
 template <class P, int TZ, int TY, int MAT>
 static void launch_tma_mat(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     const dim3 block(TZ, TY, 1);
@@ -92,11 +113,8 @@ static void launch_epilogue(Plan &p, bool is_E, const double *wave, cudaStream_t
                 break;
             }
             case EPI_PML: {
-                const SlabK &S = g.slab[op.slab];
-                const long cells = (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) *
-                                   (S.axis == 2 ? S.th : g.nz);
-                if (is_E) k_pml_slab<P, true><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, op.slab);
-                else k_pml_slab<P, false><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, op.slab);
+                if (is_E) launch_pml_slab<P, true>(g, op.slab, st);
+                else launch_pml_slab<P, false>(g, op.slab, st);
                 break;
             }
             case EPI_SOFT: {
