@@ -196,8 +196,8 @@ def traffic_from_profile(precision, n, half, materials, automatic_plan):
     committed ncu summary, if it covers this precision, material layout and
     (automatic) plan."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
-    if (not os.path.exists(path) or not automatic_plan
-            or materials != {"E": ["index", 3], "H": ["uniform", 1]}):
+    if (not os.path.exists(path) or not automatic_plan or materials["E"] is None or materials["H"] is None
+            or (materials["E"][0], materials["H"][0]) != ("index", "uniform")):
         return None
     with open(path) as f:
         d = json.load(f)

@@ -117,6 +117,7 @@ SIGNATURES = {
     "fdtd_plan_create": (c_int32, [ctypes.POINTER(GridDesc), ctypes.POINTER(c_void_p)]),
     "fdtd_plan_destroy": (c_int32, [c_void_p]),
     "fdtd_plan_status": (c_int32, [c_void_p, ctypes.POINTER(c_int32), c_int32, c_void_p]),
+    "fdtd_selftest_bounded_wait": (c_int32, [ctypes.c_uint32, ctypes.POINTER(c_int32), c_void_p]),
     "fdtd_run": (c_int32, [c_void_p, ctypes.POINTER(RunArgs), c_void_p]),
     "fdtd_run_capture": (c_int32, [c_void_p, ctypes.POINTER(RunArgs), ctypes.POINTER(CaptureArgs), c_void_p]),
     "fdtd_adjoint_run": (c_int32, [c_void_p, ctypes.POINTER(AdjointArgs), c_void_p]),

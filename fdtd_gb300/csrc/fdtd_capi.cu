@@ -726,6 +726,26 @@ int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t
     return FDTD_OK;
 }
 
+int fdtd_selftest_bounded_wait(uint32_t polls, int32_t *status_out, fdtd_stream_t stream) {
+    if (!status_out) return FDTD_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    int *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e);
+    int v = 0;
+    e = cudaMemsetAsync(d, 0, sizeof(int), st);
+    if (e == cudaSuccess) {
+        launch_wait_selftest(d, polls, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&v, d, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e);
+    *status_out = v;
+    return FDTD_OK;
+}
+
 int fdtd_run(fdtd_plan *plan, const fdtd_run_args *args, fdtd_stream_t stream) {
     if (!plan || !args) return FDTD_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;

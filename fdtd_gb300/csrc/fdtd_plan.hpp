@@ -74,6 +74,10 @@ int adjoint_f64(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st);
 // Stage size in bytes of the TMA-staged kernels for a precision, tile rows
 // and the material modes of the E and H passes (the larger of the two).
 size_t tma_stage_bytes(int precision, int tile_rows, int mat_E, int mat_H);
+
+// One CTA waiting (bounded) on an mbarrier nothing arrives at; sets bit 0 of
+// *status (device) on expiry.
+void launch_wait_selftest(int *status, unsigned limit, cudaStream_t st);
 // Tensor maps and the shared-memory attribute of the TMA-staged kernels.
 int prepare_tma_f32(Plan &p);
 int prepare_tma_f32c(Plan &p);

@@ -42,22 +42,32 @@ _MAX_TABLE = 256  # distinct value triples a one-byte material index can address
 
 def compact_material(x, chunk=1 << 25, index_ok=True):
     """Compact copy of a (nx, ny, nz, 3) inverse-material array for the staged
-    passes: ``(table, index)`` with ``table`` the (n, 3) distinct value triples
-    and ``index`` the uint8 (nx, ny, nz) row of every cell, or ``(table, None)``
-    when every cell holds the same triple; ``None`` when there are more than 256
-    triples, or more than one and ``index_ok`` is false.  Values are compared as
-    bit patterns, so signed zeros and NaN payloads keep their table rows and
-    ``table[index] == x`` holds bit for bit.  One pass decides uniformity; the
-    distinct values of each component come from a strided sample, checked
-    against every cell by binary search (a sort of the missing values only
-    when the sample missed some)."""
+    passes: ``(table, index)`` with ``table`` an (n, 3) array of value triples
+    and ``index`` the uint8 (nx, ny, nz) table row of every cell, or
+    ``(table, None)`` when every cell holds the same triple; ``None`` when the
+    cells hold more than 256 distinct triples, or more than one and
+    ``index_ok`` is false.  Values are compared as bit patterns, so signed
+    zeros and NaN payloads keep their own rows and ``table[index] == x`` holds
+    bit for bit.
+
+    One pass decides uniformity.  The distinct values of each component are
+    taken from a strided sample and one more pass finds every cell's value by
+    binary search, forming its key (the mixed-radix number of its three value
+    positions); only if the sample missed a value are the components sorted
+    in full.  When the product of the three value counts is at most 256 the
+    key is the index (the table lists every combination); otherwise the keys
+    present are ranked."""
     itype = torch.int32 if x.element_size() == 4 else torch.int64
+    dev = x.device
     bits = x.contiguous().view(itype).reshape(-1, 3)
     ncell = bits.shape[0]
     if ncell == 0:
         return None
     first = bits[:1]
-    if all(bool((bits[a:a + chunk] == first).all()) for a in range(0, ncell, chunk)):
+    differs = torch.zeros((), dtype=torch.bool, device=dev)
+    for a in range(0, ncell, chunk):
+        differs |= (bits[a:a + chunk] != first).any()
+    if not bool(differs):
         return x.reshape(-1, 3)[:1].clone(), None
     if not index_ok:
         return None
@@ -65,42 +75,47 @@ def compact_material(x, chunk=1 << 25, index_ok=True):
     sample = bits[::max(1, ncell // 65536)]
     if torch.unique(sample, dim=0).shape[0] > _MAX_TABLE:
         return None
-    comps = []
-    for c in range(3):
-        u = torch.unique(sample[:, c])
-        missing = []
-        for a in range(0, ncell, chunk):
-            col = bits[a:a + chunk, c].contiguous()
-            pos = torch.searchsorted(u, col).clamp_(max=u.numel() - 1)
-            bad = u[pos] != col
-            if bool(bad.any()):
-                missing.append(torch.unique(col[bad]))
-                if sum(m.numel() for m in missing) > _MAX_TABLE:
-                    return None
-        if missing:
-            u = torch.unique(torch.cat([u] + missing))
-        if u.numel() > _MAX_TABLE:
+    comps = [torch.unique(sample[:, c]) for c in range(3)]
+    key = torch.empty(ncell, dtype=torch.int32, device=dev)
+    for attempt in range(2):
+        sizes = [u.numel() for u in comps]
+        if max(sizes) > _MAX_TABLE:
             return None
-        comps.append(u)
+        missed = torch.zeros((), dtype=torch.bool, device=dev)
+        for a in range(0, ncell, chunk):
+            k = None
+            for c in range(3):
+                col = bits[a:a + chunk, c].contiguous()
+                pos = torch.searchsorted(comps[c], col).clamp_(max=sizes[c] - 1)
+                missed |= (comps[c][pos] != col).any()
+                pos = pos.to(torch.int32)
+                k = pos if k is None else k * sizes[c] + pos
+            key[a:a + chunk] = k
+        if not bool(missed):
+            break
+        if attempt == 1:
+            raise AssertionError("material values missing after a full sort")
+        # the sample missed some values: every distinct value, by sorting
+        comps = []
+        for c in range(3):
+            parts = [torch.unique(bits[a:a + chunk, c]) for a in range(0, ncell, chunk)]
+            comps.append(torch.unique(torch.cat(parts)) if len(parts) > 1 else parts[0])
     n0, n1, n2 = (u.numel() for u in comps)
-
-    def keys(a):
-        blk = bits[a:a + chunk]
-        k = torch.searchsorted(comps[0], blk[:, 0].contiguous())
-        k = k * n1 + torch.searchsorted(comps[1], blk[:, 1].contiguous())
-        return k * n2 + torch.searchsorted(comps[2], blk[:, 2].contiguous())
-
-    present = torch.zeros(n0 * n1 * n2, dtype=torch.bool, device=x.device)
-    for a in range(0, ncell, chunk):
-        present[keys(a)] = True
-    rows = torch.nonzero(present).reshape(-1)
-    if rows.numel() > _MAX_TABLE:
-        return None
-    rank = torch.zeros(n0 * n1 * n2, dtype=torch.uint8, device=x.device)
-    rank[rows] = torch.arange(rows.numel(), device=x.device).to(torch.uint8)
-    index = torch.empty(ncell, dtype=torch.uint8, device=x.device)
-    for a in range(0, ncell, chunk):
-        index[a:a + chunk] = rank[keys(a)]
+    combos = n0 * n1 * n2
+    if combos <= _MAX_TABLE:
+        rows = torch.arange(combos, device=dev)
+        index = key.to(torch.uint8)
+    else:
+        present = torch.zeros(combos, dtype=torch.bool, device=dev)
+        present[key.long()] = True
+        rows = torch.nonzero(present).reshape(-1)
+        if rows.numel() > _MAX_TABLE:
+            return None
+        rank = torch.zeros(combos, dtype=torch.uint8, device=dev)
+        rank[rows] = torch.arange(rows.numel(), device=dev).to(torch.uint8)
+        index = torch.empty(ncell, dtype=torch.uint8, device=dev)
+        for a in range(0, ncell, chunk):
+            index[a:a + chunk] = rank[key[a:a + chunk].long()]
     i2 = rows % n2
     i1 = (rows // n2) % n1
     i0 = rows // (n1 * n2)

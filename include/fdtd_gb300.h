@@ -220,6 +220,13 @@ int fdtd_plan_destroy(fdtd_plan *plan);
  * reference counterpart (the reference cannot fail this way). */
 int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t stream);
 
+/* Device check of the staged passes' failure path; no counterpart in the
+ * reference.  One CTA waits on an mbarrier that nothing arrives at, giving up
+ * after `polls` polls (the staged passes use the same bounded wait), and sets
+ * bit 0 of a status word on expiry, which *status_out receives (1 expected).
+ * Nothing faults; the context stays usable.  Synchronises `stream`. */
+int fdtd_selftest_bounded_wait(uint32_t polls, int32_t *status_out, fdtd_stream_t stream);
+
 /* Grid.run / Grid.step / Grid.update_E / Grid.update_H
  * (fdtd/grid.py:250-325): n_steps steps (or one half step) with detector
  * sampling and DFT accumulation after each half step. */

@@ -30,7 +30,8 @@ def test_round_trip_few_triples(dtype):
     x[0, 0, 0, 1] = -0.0
     table, index = compact_material(x, chunk=97)
     assert index.dtype == torch.uint8 and index.shape == (9, 10, 16)
-    assert table.dtype == dtype and table.shape[1] == 3 and table.shape[0] <= 9
+    assert table.dtype == dtype and table.shape[1] == 3 and table.shape[0] <= 256
+    assert torch.unique(index).numel() <= 9
     back = _expand((table, index), x.shape)
     itype = torch.int32 if dtype == torch.float32 else torch.int64
     assert torch.equal(back.view(itype), x.view(itype))  # bit patterns, -0.0 included
@@ -84,4 +85,16 @@ def test_values_the_sample_misses():
     x[63, 63, 31, 2] = -0.0
     table, index = compact_material(x, chunk=5000)
     assert torch.equal(table[index.long()].view(torch.int32), x.view(torch.int32))
-    assert table.shape[0] == 4
+    assert torch.unique(index).numel() == 4
+
+
+def test_every_combination_table():
+    """Few values per component: the table lists every combination of them
+    (here 2 x 2 x 1) and the index is the combination's number."""
+    x = torch.zeros((4, 4, 16, 3), dtype=torch.float32)
+    x[..., 0] = 1.0
+    x[:2, ..., 0] = 2.0
+    x[:, :2, :, 1] = 5.0
+    table, index = compact_material(x)
+    assert table.shape == (4, 3)
+    assert torch.equal(table[index.long()], x)
