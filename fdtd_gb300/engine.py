@@ -345,7 +345,8 @@ class Engine:
         if g.precision == "float64":
             if self._scaled is None or self._scaled[0].shape != g._inverse_permittivity.shape:
                 self._scaled = (torch.empty_like(g._inverse_permittivity), torch.empty_like(g._inverse_permeability))
-            self._scaled_keys = [None, None]
+                self._compact_keys = [None, None]  # new arrays: fill and encode them afresh
+                self._scaled_keys = [None, None]
             self._sync_scaled_materials()
             d.inv_eps, d.inv_mu = self._scaled[0].data_ptr(), self._scaled[1].data_ptr()
             d.materials_scaled = 1
@@ -353,8 +354,7 @@ class Engine:
             self._scaled = None
             d.inv_eps = g._inverse_permittivity.data_ptr()
             d.inv_mu = g._inverse_permeability.data_ptr()
-        self._compact_keys = [None, None]
-        self._compact = [None, None]
+        # compact copies: re-encoded only if the arrays changed since the last plan
         self._sync_compact_materials()
         for enc, tab, n, idx in ((self._compact[0], "eps_table", "n_eps_table", "eps_index"),
                                  (self._compact[1], "mu_table", "n_mu_table", "mu_index")):
