@@ -435,11 +435,11 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         t.XC = d->x_chunk;
     } else {
         // register kernels: split x only when the (z, y) columns do not give
-        // two waves of CTAs.  Staged kernels (one CTA per SM): about twenty
-        // waves, so the partly filled last wave costs little (measured on
-        // 768^3: 3.8 waves 58.7, 7.6 waves 61.4, 22.7 waves 63.1 Gcell/s), with
-        // at least 32 planes per chunk (a chunk refills the ring and re-reads
-        // one halo plane)
+        // two waves of CTAs.  Staged kernels: about twenty waves of the
+        // resident CTAs, so the partly filled last wave costs little
+        // (measured on 768^3 with one CTA per SM: 3.8 waves 58.7, 7.6 waves
+        // 61.4, 22.7 waves 63.1 Gcell/s), with at least 32 planes per chunk (a
+        // chunk refills the ring and re-reads one halo plane)
         const long cols = (long)t.gz * t.gy;
         const long target = (use_tma ? 20L : 2L) * n_sm * ctas_per_sm;
         long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
