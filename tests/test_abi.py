@@ -7,6 +7,7 @@ import os
 import re
 
 import pytest
+import torch
 
 from fdtd_gb300 import _native
 
@@ -65,3 +66,34 @@ def test_argument_errors_without_gpu(lib):
     assert lib.fdtd_run(None, None, None) == 1
     assert lib.fdtd_curl_E(0, None, None, 1, 1, 1, None) == 1
     assert lib.fdtd_field_stats(None, None, None, None) == 1
+
+
+def test_compact_material_arguments_without_gpu(lib):
+    """The compact material fields are validated before any CUDA call: at most
+    256 table rows, a table for any count, an index unless the table has one
+    row; an unaligned index or nz not a multiple of 16 is not an error (the
+    plan reads the full arrays)."""
+    if torch.cuda.is_available():
+        pytest.skip("checks the CPU-only path")
+    fake = 1 << 20  # never dereferenced: validation fails or the first CUDA call does
+
+    def desc(**kw):
+        d = _native.GridDesc()
+        d.abi_version = _native.ABI_VERSION
+        d.precision = _native.FLOAT32
+        d.nx = d.ny = d.nz = 16
+        d.courant = 0.5
+        d.E = d.H = d.inv_eps = d.inv_mu = fake
+        for k, v in kw.items():
+            setattr(d, k, v)
+        return d
+
+    plan = ctypes.c_void_p()
+    create = lambda d: lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan))  # noqa: E731
+    assert create(desc(n_eps_table=257, eps_table=fake, eps_index=fake)) == 1
+    assert create(desc(n_eps_table=-1)) == 1
+    assert create(desc(n_eps_table=2, eps_table=fake)) == 1  # no index for two rows
+    assert create(desc(n_mu_table=1)) == 1  # no table
+    assert create(desc(materials_scaled=1)) == 2  # float64 plans only
+    # valid compact fields pass validation; the CPU-only host then fails at the first CUDA call
+    assert create(desc(n_eps_table=3, eps_table=fake, eps_index=fake, n_mu_table=1, mu_table=fake)) == 3
