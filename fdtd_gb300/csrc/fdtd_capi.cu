@@ -248,9 +248,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // The automatic choice therefore keeps only leading y slabs, for float32
     // with compact materials.
     const long ncell = (long)d->nx * d->ny * d->nz;
+    // 2D grids (nz = 1) of 8M cells and more split too (8192^2 float32: 63.1
+    // vs 58.0 Gcell/s with 32-plane chunks)
     p.pml_split = g.nslab > 0 &&
-                  (d->pml_mode >= 2 || (d->pml_mode == 0 && vec && (long)d->nz * 3 * (long)esize >= 768 &&
-                                        ncell >= (8L << 20)));
+                  (d->pml_mode >= 2 ||
+                   (d->pml_mode == 0 && ncell >= (8L << 20) &&
+                    ((vec && (long)d->nz * 3 * (long)esize >= 768) || d->nz == 1)));
     int kfs = 0;  // leading slabs kept in the fused pass when split
     const bool auto_keep = d->pml_mode == 0 && d->precision == FDTD_FLOAT32 && mat_want[0] != MAT_FULL &&
                            mat_want[1] != MAT_FULL;
@@ -434,18 +437,23 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (d->x_chunk > 0) {
         t.XC = d->x_chunk;
     } else {
-        // register kernels: split x only when the (z, y) columns do not give
-        // two waves of CTAs.  Staged kernels: about twenty waves of the
-        // resident CTAs, so the partly filled last wave costs little
-        // (measured on 768^3 with one CTA per SM: 3.8 waves 58.7, 7.6 waves
-        // 61.4, 22.7 waves 63.1 Gcell/s), with at least 32 planes per chunk (a
-        // chunk refills the ring and re-reads one halo plane)
+        // Staged kernels: about twenty waves of the resident CTAs, so the
+        // partly filled last wave costs little (measured on 768^3 with one CTA
+        // per SM: 3.8 waves 58.7, 7.6 waves 61.4, 22.7 waves 63.1 Gcell/s),
+        // with at least 32 planes per chunk (a chunk refills the ring and
+        // re-reads one halo plane).  Register kernels: about thirty-two waves
+        // (2D 8192^2 float32: 2 waves 39.5, 27 waves 58.0, 54 waves 59.4
+        // Gcell/s), with chunks of at least 32 planes while those still give
+        // eight waves; small grids take shorter chunks (config 4, 128^3: one
+        // plane per chunk 20.9 vs 19.3 Gcell/s with four)
         const long cols = (long)t.gz * t.gy;
-        const long target = (use_tma ? 20L : 2L) * n_sm * ctas_per_sm;
+        const long wave = (long)n_sm * ctas_per_sm;
+        const long target = (use_tma ? 20L : 32L) * wave;
         long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
         const long max_chunks = use_tma ? std::max(1L, (long)d->nx / 32) : (long)d->nx;
         chunks = std::max(1L, std::min(chunks, max_chunks));
         t.XC = (int)((d->nx + chunks - 1) / chunks);
+        if (!use_tma && t.XC < 32 && d->nx >= 32 && cols * ((d->nx + 31) / 32) >= 8 * wave) t.XC = 32;
     }
     t.gx = (d->nx + t.XC - 1) / t.XC;
     if (t.gx > 65535) return FDTD_ERR_UNSUPPORTED;
@@ -456,10 +464,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         const int TZ = std::min(32, next_pow2(zt));
         const int TY = kThreads / TZ;
         const int gz = (zt + TZ - 1) / TZ, gy = (d->ny + TY - 1) / TY;
-        const long cols = (long)gz * gy, target = 4L * n_sm;
+        // x chunks as for the register-streaming forward kernels
+        const long cols = (long)gz * gy, wave = 2L * n_sm, target = 32L * wave;
         long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
         chunks = std::max(1L, std::min(chunks, (long)d->nx));
-        const int XC = (int)((d->nx + chunks - 1) / chunks);
+        int XC = (int)((d->nx + chunks - 1) / chunks);
+        if (XC < 32 && d->nx >= 32 && cols * ((d->nx + 31) / 32) >= 8 * wave) XC = 32;
         p.adj_V = V;
         p.adj_TZ = TZ;
         p.adj_TY = TY;
