@@ -48,41 +48,96 @@ __device__ __forceinline__ unsigned slab_mask_x(const GridK &g, int i) {
 
 // Objects of one cell (fdtd/objects.py:118-277), in registration order.
 template <class P>
-__device__ __forceinline__ void apply_objects(const GridK &g, int i, int j, int k, typename P::T c, typename P::T cu0,
-                                              typename P::T cu1, typename P::T cu2, typename P::T &ex,
-                                              typename P::T &ey, typename P::T &ez, typename P::T &lx,
-                                              typename P::T &ly, typename P::T &lz, int ob0, int ob1) {
+__device__ __forceinline__ void apply_object_cell(const ItemK &o, size_t li, typename P::T c, typename P::T cu0,
+                                                  typename P::T cu1, typename P::T cu2, typename P::T &ex,
+                                                  typename P::T &ey, typename P::T &ez, typename P::T &lx,
+                                                  typename P::T &ly, typename P::T &lz) {
+    using T = typename P::T;
+    if (o.kind == FDTD_ITEM_OBJECT) {
+        const T *cf = (const T *)o.coef[0] + 3 * li;
+        P::add_prod(ex, lx, cf[0], cu0);
+        P::add_prod(ey, ly, cf[1], cu1);
+        P::add_prod(ez, lz, cf[2], cu2);
+    } else if (o.kind == FDTD_ITEM_ABSORBING) {
+        const T *r = (const T *)o.coef[0] + 3 * li;
+        const T *ci = (const T *)o.coef[1] + 3 * li;
+        P::scale(ex, lx, r[0]);
+        P::scale(ey, ly, r[1]);
+        P::scale(ez, lz, r[2]);
+        if constexpr (sizeof(T) == 4) {
+            P::add_prod(ex, lx, ci[0], cu0);
+            P::add_prod(ey, ly, ci[1], cu1);
+            P::add_prod(ez, lz, ci[2], cu2);
+        } else {
+            const T *opf = (const T *)o.coef[2] + 3 * li;
+            P::add_quot(ex, lx, ci[0], cu0, opf[0]);
+            P::add_quot(ey, ly, ci[1], cu1, opf[1]);
+            P::add_quot(ez, lz, ci[2], cu2, opf[2]);
+        }
+    } else {
+        const T *M = (const T *)o.coef[0] + 9 * li;
+        P::add_prod(ex, lx, c, P::dot3(M[0], M[1], M[2], cu0, cu1, cu2));
+        P::add_prod(ey, ly, c, P::dot3(M[3], M[4], M[5], cu0, cu1, cu2));
+        P::add_prod(ez, lz, c, P::dot3(M[6], M[7], M[8], cu0, cu1, cu2));
+    }
+}
+
+__device__ __forceinline__ bool aligned16_ptr(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+// Objects of a thread's V cells (fdtd/objects.py:92-129, 198-221, 256-269),
+// items in list order; each cell gets the same operations in the same order
+// as one at a time.  Where all V cells lie in a box and their coefficients
+// start on a 16-byte boundary they are read with 16-byte loads: one 4- or
+// 8-byte load per value at a 3- or 9-value stride touches a sector per lane,
+// and the CTAs holding a 1.6 % anisotropic box (config 5) took twice as long
+// per plane as the others.
+template <class P, int V>
+__device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, int k0, typename P::T c,
+                                                const typename P::T (&cu)[3][V], typename P::T (&e)[3 * V],
+                                                typename P::T (&el)[3 * V], int ob0, int ob1) {
     using T = typename P::T;
     for (int it = ob0; it < ob1; ++it) {
         const ItemK &o = g.items[g.obj_idx[it]];
-        if (!in_box(o, i, j, k)) continue;
-        const size_t li = box_index(o, i, j, k);
-        if (o.kind == FDTD_ITEM_OBJECT) {
-            const T *cf = (const T *)o.coef[0] + 3 * li;
-            P::add_prod(ex, lx, cf[0], cu0);
-            P::add_prod(ey, ly, cf[1], cu1);
-            P::add_prod(ez, lz, cf[2], cu2);
-        } else if (o.kind == FDTD_ITEM_ABSORBING) {
-            const T *r = (const T *)o.coef[0] + 3 * li;
-            const T *ci = (const T *)o.coef[1] + 3 * li;
-            P::scale(ex, lx, r[0]);
-            P::scale(ey, ly, r[1]);
-            P::scale(ez, lz, r[2]);
-            if constexpr (sizeof(T) == 4) {
-                P::add_prod(ex, lx, ci[0], cu0);
-                P::add_prod(ey, ly, ci[1], cu1);
-                P::add_prod(ez, lz, ci[2], cu2);
-            } else {
-                const T *opf = (const T *)o.coef[2] + 3 * li;
-                P::add_quot(ex, lx, ci[0], cu0, opf[0]);
-                P::add_quot(ey, ly, ci[1], cu1, opf[1]);
-                P::add_quot(ez, lz, ci[2], cu2, opf[2]);
+        if (i < o.lo[0] || i >= o.hi[0] || j < o.lo[1] || j >= o.hi[1] || k0 >= o.hi[2] || k0 + V <= o.lo[2])
+            continue;
+        if constexpr (V > 1) {
+            const size_t li = k0 >= o.lo[2] ? box_index(o, i, j, k0) : 0;
+            const bool whole = k0 >= o.lo[2] && k0 + V <= o.hi[2];
+            if (whole && o.kind == FDTD_ITEM_ANISOTROPIC) {
+                const T *src = (const T *)o.coef[0] + 9 * li;
+                if (aligned16_ptr(src)) {
+                    alignas(16) T M[9 * V];
+                    ld_vec_ro(M, src);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        const T *m = M + 9 * v;
+                        P::add_prod(e[3 * v], el[3 * v], c, P::dot3(m[0], m[1], m[2], cu[0][v], cu[1][v], cu[2][v]));
+                        P::add_prod(e[3 * v + 1], el[3 * v + 1], c,
+                                    P::dot3(m[3], m[4], m[5], cu[0][v], cu[1][v], cu[2][v]));
+                        P::add_prod(e[3 * v + 2], el[3 * v + 2], c,
+                                    P::dot3(m[6], m[7], m[8], cu[0][v], cu[1][v], cu[2][v]));
+                    }
+                    continue;
+                }
+            } else if (whole && o.kind == FDTD_ITEM_OBJECT) {
+                const T *src = (const T *)o.coef[0] + 3 * li;
+                if (aligned16_ptr(src)) {
+                    alignas(16) T cf[3 * V];
+                    ld_vec_ro(cf, src);
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) P::add_prod(e[3 * v + q], el[3 * v + q], cf[3 * v + q], cu[q][v]);
+                    continue;
+                }
             }
-        } else {
-            const T *M = (const T *)o.coef[0] + 9 * li;
-            P::add_prod(ex, lx, c, P::dot3(M[0], M[1], M[2], cu0, cu1, cu2));
-            P::add_prod(ey, ly, c, P::dot3(M[3], M[4], M[5], cu0, cu1, cu2));
-            P::add_prod(ez, lz, c, P::dot3(M[6], M[7], M[8], cu0, cu1, cu2));
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int k = k0 + v;
+            if (k < o.lo[2] || k >= o.hi[2]) continue;
+            apply_object_cell<P>(o, box_index(o, i, j, k), c, cu[0][v], cu[1][v], cu[2][v], e[3 * v], e[3 * v + 1],
+                                 e[3 * v + 2], el[3 * v], el[3 * v + 1], el[3 * v + 2]);
         }
     }
 }
@@ -249,6 +304,7 @@ __device__ __forceinline__ void thread_E(const GridK &g, const double *__restric
                                          int sb0, int sb1, const PsiSrc<typename P::T> &src, unsigned slabs) {
     using T = typename P::T;
     T d[6][V];  // dxHy, dxHz, dyHx, dyHz, dzHx, dzHy (backward, zero on the first plane)
+    T cu[3][V];  // curl H
 #pragma unroll
     for (int v = 0; v < V; ++v) {
         const int k = k0 + v;
@@ -261,16 +317,14 @@ __device__ __forceinline__ void thread_E(const GridK &g, const double *__restric
         d[3][v] = (j > 0) ? hz - hj[3 * v + 2] : T(0);
         d[4][v] = (k > 0) ? hx - pkx : T(0);
         d[5][v] = (k > 0) ? hy - pky : T(0);
-        const T cu0 = d[3][v] - d[5][v];
-        const T cu1 = d[4][v] - d[1][v];
-        const T cu2 = d[0][v] - d[2][v];
-        P::add_prod(e[3 * v], el[3 * v], P::cm(c, m[3 * v]), cu0);
-        P::add_prod(e[3 * v + 1], el[3 * v + 1], P::cm(c, m[3 * v + 1]), cu1);
-        P::add_prod(e[3 * v + 2], el[3 * v + 2], P::cm(c, m[3 * v + 2]), cu2);
-        if (ob0 < ob1)
-            apply_objects<P>(g, i, j, k, c, cu0, cu1, cu2, e[3 * v], e[3 * v + 1], e[3 * v + 2], el[3 * v],
-                             el[3 * v + 1], el[3 * v + 2], ob0, ob1);
+        cu[0][v] = d[3][v] - d[5][v];
+        cu[1][v] = d[4][v] - d[1][v];
+        cu[2][v] = d[0][v] - d[2][v];
+        P::add_prod(e[3 * v], el[3 * v], P::cm(c, m[3 * v]), cu[0][v]);
+        P::add_prod(e[3 * v + 1], el[3 * v + 1], P::cm(c, m[3 * v + 1]), cu[1][v]);
+        P::add_prod(e[3 * v + 2], el[3 * v + 2], P::cm(c, m[3 * v + 2]), cu[2][v]);
     }
+    if (ob0 < ob1) apply_objects_v<P, V>(g, i, j, k0, c, cu, e, el, ob0, ob1);
     if (slabs) apply_pml<P, V, true>(g, i, j, k0, c, d, m, e, el, src, slabs);
 #pragma unroll
     for (int v = 0; v < V; ++v) {

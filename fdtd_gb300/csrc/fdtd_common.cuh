@@ -37,13 +37,13 @@ struct ItemK {
     int aux;  // FDTD_ITEM_FEEDBACK: its point in the current-probe list
 };
 
-// Everything a half-step kernel needs, passed by value.
 // Material modes of a staged pass: the inverse material read per cell as
 // three values (MAT_FULL), as a one-byte index into a small table of value
 // triples (MAT_IDS), or not at all when every cell has the same triple
 // (MAT_UNIFORM).  The values and the arithmetic are the same in every mode.
 constexpr int MAT_FULL = 0, MAT_IDS = 1, MAT_UNIFORM = 2;
 
+// Everything a half-step kernel needs, passed by value.
 struct GridK {
     int nx, ny, nz;
     double courant;
