@@ -130,6 +130,30 @@ __device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, in
                         for (int q = 0; q < 3; ++q) P::add_prod(e[3 * v + q], el[3 * v + q], cf[3 * v + q], cu[q][v]);
                     continue;
                 }
+            } else if (whole && o.kind == FDTD_ITEM_ABSORBING) {
+                const T *rs = (const T *)o.coef[0] + 3 * li, *cs = (const T *)o.coef[1] + 3 * li;
+                const T *os = sizeof(T) == 8 ? (const T *)o.coef[2] + 3 * li : rs;
+                if (aligned16_ptr(rs) && aligned16_ptr(cs) && aligned16_ptr(os)) {
+                    alignas(16) T r[3 * V], ci[3 * V];
+                    ld_vec_ro(r, rs);
+                    ld_vec_ro(ci, cs);
+                    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+                        for (int q = 0; q < 3 * V; ++q) {
+                            P::scale(e[q], el[q], r[q]);
+                            P::add_prod(e[q], el[q], ci[q], cu[q % 3][q / 3]);
+                        }
+                    } else {
+                        alignas(16) T opf[3 * V];
+                        ld_vec_ro(opf, os);
+#pragma unroll
+                        for (int q = 0; q < 3 * V; ++q) {
+                            P::scale(e[q], el[q], r[q]);
+                            P::add_quot(e[q], el[q], ci[q], cu[q % 3][q / 3], opf[q]);
+                        }
+                    }
+                    continue;
+                }
             }
         }
 #pragma unroll
