@@ -9,6 +9,8 @@ float32 1e-4 relative L2).  In-place changes of the materials between runs
 must be followed.
 """
 
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -147,3 +149,69 @@ def test_in_place_material_changes_are_followed(fd, precision):
     assert rel_l2(g.E, o.E) <= TOL[precision] and rel_l2(g.H, o.H) <= TOL[precision]
     for d, od in zip(g.detectors, o.detectors):
         assert rel_l2(np.asarray(d.E), np.stack(od.E)) <= TOL[precision]
+
+
+def _raw_run(lib, fields, ie, imu, steps, eps_compact=None, mu_compact=None):
+    """Plan through the C ABI with the given material arrays (and compact
+    copies), `steps` steps from the given fields; returns (E, H)."""
+    from fdtd_gb300 import _native
+
+    E, H = (f.clone() for f in fields)
+    d = _native.GridDesc()
+    d.abi_version = _native.ABI_VERSION
+    d.precision = _native.FLOAT32
+    d.nx, d.ny, d.nz = E.shape[:3]
+    d.courant = 0.99 / 3 ** 0.5
+    d.E, d.H, d.inv_eps, d.inv_mu = E.data_ptr(), H.data_ptr(), ie.data_ptr(), imu.data_ptr()
+    d.variant = 2
+    for enc, tab, n, idx in ((eps_compact, "eps_table", "n_eps_table", "eps_index"),
+                             (mu_compact, "mu_table", "n_mu_table", "mu_index")):
+        if enc is not None:
+            setattr(d, tab, enc[0].data_ptr())
+            setattr(d, n, enc[0].shape[0])
+            setattr(d, idx, enc[1].data_ptr() if enc[1] is not None else None)
+    plan = ctypes.c_void_p()
+    assert lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan)) == 0
+    try:
+        a = _native.RunArgs()
+        a.n_steps = steps
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        assert lib.fdtd_run(plan, ctypes.byref(a), stream) == 0
+        st = ctypes.c_int32(-1)
+        assert lib.fdtd_plan_status(plan, ctypes.byref(st), 0, stream) == 0 and st.value == 0
+        torch.cuda.synchronize()
+    finally:
+        lib.fdtd_plan_destroy(plan)
+    return E, H
+
+
+def test_c_abi_compact_fields(fd):
+    """A caller of the C ABI passing its own table and index gets the bits of
+    the full-array plan; index bytes past the table read zeros."""
+    from fdtd_gb300 import _native
+    from fdtd_gb300.engine import compact_material
+
+    lib = _native.load()
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    shape = (24, 20, 32)
+    E = torch.randn(shape + (3,), device="cuda", generator=gen)
+    H = torch.randn(shape + (3,), device="cuda", generator=gen)
+    levels = torch.tensor([1.0, 0.5, 1 / 3.0, 0.25], device="cuda")
+    ie = levels[torch.randint(0, 4, shape, device="cuda", generator=gen)][..., None].expand(shape + (3,)).contiguous()
+    imu = torch.ones(shape + (3,), device="cuda")
+    full = _raw_run(lib, (E, H), ie, imu, 12)
+    enc = compact_material(ie)
+    assert enc is not None and enc[1] is not None
+    mu_enc = compact_material(imu)
+    comp = _raw_run(lib, (E, H), ie, imu, 12, enc, mu_enc)
+    for a, b in zip(full, comp):
+        assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    # index bytes past the table: zeros, like a full array holding zeros there
+    idx = enc[1].clone()
+    idx[3:6, 4:9, 8:20] = 200
+    ie0 = ie.clone()
+    ie0[3:6, 4:9, 8:20] = 0.0
+    want = _raw_run(lib, (E, H), ie0, imu, 12)
+    got = _raw_run(lib, (E, H), ie, imu, 12, (enc[0], idx), mu_enc)
+    for a, b in zip(want, got):
+        assert torch.equal(a.view(torch.int32), b.view(torch.int32))
