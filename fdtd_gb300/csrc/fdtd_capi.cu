@@ -31,6 +31,27 @@ static int next_pow2(int v) {
 
 static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
 
+// Threads along z of a register-streaming tile for zt threads' worth of
+// cells: the next power of two up to 32, or 16 where that pads less (config 5,
+// 48 threads: 32-wide tiles leave a quarter of the threads idle).
+static int tile_width(int zt) {
+    if (zt <= 32) return next_pow2(zt);
+    const int pad32 = (zt + 31) / 32 * 32 - zt, pad16 = (zt + 15) / 16 * 16 - zt;
+    return pad16 < pad32 ? 16 : 32;
+}
+
+// Planes per CTA of the register-streaming kernels: at most 32, and fewer
+// until the grid has eight waves of CTAs (a chunk re-reads one halo plane, a
+// partly filled last wave idles SMs).  Measured: 2D 8192^2 float32, 2 waves of
+// 432-plane chunks 39.5, 27 waves of 32-plane chunks 58.0 Gcell/s; config 4
+// (128^3, 16 columns) one plane per chunk 20.9 vs 19.3 with four.
+static int register_chunk(int nx, long cols, long wave) {
+    long chunks = (8 * wave + cols - 1) / cols;
+    chunks = std::max(chunks, ((long)nx + 31) / 32);
+    chunks = std::max(1L, std::min(chunks, (long)nx));
+    return (int)((nx + chunks - 1) / chunks);
+}
+
 // Padded 4-value rows of the shared-memory material table of a staged pass.
 static int mat_lut_rows(int mat) { return mat == MAT_IDS ? 256 : (mat == MAT_UNIFORM ? 1 : 0); }
 
@@ -425,7 +446,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (!use_tma) {
         t.V = vec ? vmax : 1;
         const int zthreads0 = (d->nz + t.V - 1) / t.V;
-        t.TZ = std::min(32, next_pow2(zthreads0));
+        t.TZ = tile_width(zthreads0);
         t.TY = kThreads / t.TZ;
         g.stages = 0;
         p.variant = 1;
@@ -441,19 +462,16 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         // partly filled last wave costs little (measured on 768^3 with one CTA
         // per SM: 3.8 waves 58.7, 7.6 waves 61.4, 22.7 waves 63.1 Gcell/s),
         // with at least 32 planes per chunk (a chunk refills the ring and
-        // re-reads one halo plane).  Register kernels: about thirty-two waves
-        // (2D 8192^2 float32: 2 waves 39.5, 27 waves 58.0, 54 waves 59.4
-        // Gcell/s), with chunks of at least 32 planes while those still give
-        // eight waves; small grids take shorter chunks (config 4, 128^3: one
-        // plane per chunk 20.9 vs 19.3 Gcell/s with four)
+        // re-reads one halo plane).  Register kernels: register_chunk.
         const long cols = (long)t.gz * t.gy;
         const long wave = (long)n_sm * ctas_per_sm;
-        const long target = (use_tma ? 20L : 32L) * wave;
-        long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
-        const long max_chunks = use_tma ? std::max(1L, (long)d->nx / 32) : (long)d->nx;
-        chunks = std::max(1L, std::min(chunks, max_chunks));
-        t.XC = (int)((d->nx + chunks - 1) / chunks);
-        if (!use_tma && t.XC < 32 && d->nx >= 32 && cols * ((d->nx + 31) / 32) >= 8 * wave) t.XC = 32;
+        if (use_tma) {
+            long chunks = cols >= 20L * wave ? 1 : (20L * wave + cols - 1) / cols;
+            chunks = std::max(1L, std::min(chunks, std::max(1L, (long)d->nx / 32)));
+            t.XC = (int)((d->nx + chunks - 1) / chunks);
+        } else {
+            t.XC = register_chunk(d->nx, cols, wave);
+        }
     }
     t.gx = (d->nx + t.XC - 1) / t.XC;
     if (t.gx > 65535) return FDTD_ERR_UNSUPPORTED;
@@ -461,15 +479,11 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     {
         const int V = vec ? vmax : 1;
         const int zt = (d->nz + V - 1) / V;
-        const int TZ = std::min(32, next_pow2(zt));
+        const int TZ = tile_width(zt);
         const int TY = kThreads / TZ;
         const int gz = (zt + TZ - 1) / TZ, gy = (d->ny + TY - 1) / TY;
         // x chunks as for the register-streaming forward kernels
-        const long cols = (long)gz * gy, wave = 2L * n_sm, target = 32L * wave;
-        long chunks = cols >= target ? 1 : (target + cols - 1) / cols;
-        chunks = std::max(1L, std::min(chunks, (long)d->nx));
-        int XC = (int)((d->nx + chunks - 1) / chunks);
-        if (XC < 32 && d->nx >= 32 && cols * ((d->nx + 31) / 32) >= 8 * wave) XC = 32;
+        const int XC = register_chunk(d->nx, (long)gz * gy, 2L * n_sm);
         p.adj_V = V;
         p.adj_TZ = TZ;
         p.adj_TY = TY;
