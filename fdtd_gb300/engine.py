@@ -56,16 +56,18 @@ def compact_material(x, chunk=1 << 25, index_ok=True):
     positions); only if the sample missed a value are the components sorted
     in full.  When the product of the three value counts is at most 256 the
     key is the index (the table lists every combination); otherwise the keys
-    present are ranked."""
+    present are ranked and a last pass maps every cell's key to its rank.
+    Besides the index only per-chunk temporaries are allocated."""
     itype = torch.int32 if x.element_size() == 4 else torch.int64
     dev = x.device
     bits = x.contiguous().view(itype).reshape(-1, 3)
     ncell = bits.shape[0]
     if ncell == 0:
         return None
+    starts = range(0, ncell, chunk)
     first = bits[:1]
     differs = torch.zeros((), dtype=torch.bool, device=dev)
-    for a in range(0, ncell, chunk):
+    for a in starts:
         differs |= (bits[a:a + chunk] != first).any()
     if not bool(differs):
         return x.reshape(-1, 3)[:1].clone(), None
@@ -76,46 +78,54 @@ def compact_material(x, chunk=1 << 25, index_ok=True):
     if torch.unique(sample, dim=0).shape[0] > _MAX_TABLE:
         return None
     comps = [torch.unique(sample[:, c]) for c in range(3)]
-    key = torch.empty(ncell, dtype=torch.int32, device=dev)
-    for attempt in range(2):
-        sizes = [u.numel() for u in comps]
-        if max(sizes) > _MAX_TABLE:
-            return None
-        missed = torch.zeros((), dtype=torch.bool, device=dev)
-        for a in range(0, ncell, chunk):
-            k = None
-            for c in range(3):
-                col = bits[a:a + chunk, c].contiguous()
-                pos = torch.searchsorted(comps[c], col).clamp_(max=sizes[c] - 1)
-                missed |= (comps[c][pos] != col).any()
-                pos = pos.to(torch.int32)
-                k = pos if k is None else k * sizes[c] + pos
-            key[a:a + chunk] = k
-        if not bool(missed):
-            break
-        if attempt == 1:
-            raise AssertionError("material values missing after a full sort")
+
+    def keys(a, check=None):
+        k = None
+        for c in range(3):
+            col = bits[a:a + chunk, c].contiguous()
+            pos = torch.searchsorted(comps[c], col).clamp_(max=comps[c].numel() - 1)
+            if check is not None:
+                check |= (comps[c][pos] != col).any()
+            k = pos if k is None else k * comps[c].numel() + pos
+        return k
+
+    index = torch.empty(ncell, dtype=torch.uint8, device=dev)
+    combos = comps[0].numel() * comps[1].numel() * comps[2].numel()
+    missed = torch.zeros((), dtype=torch.bool, device=dev)
+    present = None if combos <= _MAX_TABLE else torch.zeros(combos, dtype=torch.bool, device=dev)
+    for a in starts:
+        k = keys(a, missed)
+        if present is None:
+            index[a:a + chunk] = k.to(torch.uint8)
+        else:
+            present[k] = True
+    if bool(missed):
         # the sample missed some values: every distinct value, by sorting
         comps = []
         for c in range(3):
-            parts = [torch.unique(bits[a:a + chunk, c]) for a in range(0, ncell, chunk)]
+            parts = [torch.unique(bits[a:a + chunk, c]) for a in starts]
             comps.append(torch.unique(torch.cat(parts)) if len(parts) > 1 else parts[0])
+        if max(u.numel() for u in comps) > _MAX_TABLE:
+            return None
+        combos = comps[0].numel() * comps[1].numel() * comps[2].numel()
+        present = None if combos <= _MAX_TABLE else torch.zeros(combos, dtype=torch.bool, device=dev)
+        for a in starts:
+            k = keys(a)
+            if present is None:
+                index[a:a + chunk] = k.to(torch.uint8)
+            else:
+                present[k] = True
     n0, n1, n2 = (u.numel() for u in comps)
-    combos = n0 * n1 * n2
-    if combos <= _MAX_TABLE:
+    if present is None:
         rows = torch.arange(combos, device=dev)
-        index = key.to(torch.uint8)
     else:
-        present = torch.zeros(combos, dtype=torch.bool, device=dev)
-        present[key.long()] = True
         rows = torch.nonzero(present).reshape(-1)
         if rows.numel() > _MAX_TABLE:
             return None
         rank = torch.zeros(combos, dtype=torch.uint8, device=dev)
         rank[rows] = torch.arange(rows.numel(), device=dev).to(torch.uint8)
-        index = torch.empty(ncell, dtype=torch.uint8, device=dev)
-        for a in range(0, ncell, chunk):
-            index[a:a + chunk] = rank[key[a:a + chunk].long()]
+        for a in starts:
+            index[a:a + chunk] = rank[keys(a)]
     i2 = rows % n2
     i1 = (rows // n2) % n1
     i0 = rows // (n1 * n2)
@@ -231,8 +241,14 @@ class Engine:
             key = (src.data_ptr(), src._version, want)
             if self._compact_keys[q] == key:
                 continue
-            # index maps are read by TMA in rows of nz bytes: nz a multiple of 16
-            enc = compact_material(src, index_ok=g.Nz % 16 == 0) if want else None
+            # index maps are read by TMA in rows of nz bytes: nz a multiple of 16;
+            # without the memory for the copy the plan reads the full arrays
+            enc = None
+            if want:
+                try:
+                    enc = compact_material(src, index_ok=g.Nz % 16 == 0)
+                except torch.cuda.OutOfMemoryError:
+                    enc = None
             old = self._compact[q]
             if enc is not None and old is not None and self._layout(enc) == self._layout(old):
                 old[0].copy_(enc[0])
