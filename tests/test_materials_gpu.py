@@ -215,3 +215,23 @@ def test_c_abi_compact_fields(fd):
     got = _raw_run(lib, (E, H), ie, imu, 12, (enc[0], idx), mu_enc)
     for a, b in zip(want, got):
         assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+
+
+@pytest.mark.parametrize("precision", ["float32", "float64"])
+def test_half_steps_with_writes_between(fd, precision):
+    """Half-step API on a staged plan with compact materials and the y slabs
+    kept in the fused pass: writes into E between the halves are seen by the
+    H half (tests/test_detectors.py:62-70 of the reference does this)."""
+    fd.set_backend("gb300." + precision)
+    g, o = scene(fd), scene(fo)
+    eng = g._ensure_engine()
+    eng.set_tuning(variant=2, tile_rows=8, pml_mode=3)
+    assert eng.compact_materials()[0][0] == "index"
+    for q in range(6):
+        for grid in (g, o):
+            grid.update_E()
+            grid.E[9, 8, 17, 2] = 0.25 * (q + 1)
+            grid.update_H()
+            grid.time_steps_passed += 1
+    eng.check_status()
+    assert rel_l2(g.E, o.E) <= TOL[precision] and rel_l2(g.H, o.H) <= TOL[precision]
