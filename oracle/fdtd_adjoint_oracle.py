@@ -113,6 +113,8 @@ def _correct_T(pml, side, mu, lam):
 
 
 def _periodic_T(bnd, side, lam):
+    if lam.shape[bnd.axis] <= 1:
+        return  # the copy of a one-plane axis is the identity, and so is its transpose
     if side == "E":  # E[0] = E[-1]
         lam[bnd._plane(-1)] += lam[bnd._plane(0)]
         lam[bnd._plane(0)] = 0.0

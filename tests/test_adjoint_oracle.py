@@ -44,3 +44,45 @@ def test_adjoint_oracle_matches_reference_autograd(name):
     assert abs(loss - float(ref["loss"])) <= 1e-12 * abs(float(ref["loss"]))
     err = np.linalg.norm(grad - ref["grad"]) / np.linalg.norm(ref["grad"])
     assert err <= 1e-11, err
+
+
+def _plane_periodic_scene(design):
+    grid = fo.Grid((12, 10, 1), grid_spacing=100e-9)
+    grid[:, 0, :] = fo.PeriodicBoundary()
+    grid[:, :, 0] = fo.PeriodicBoundary()  # one plane: the copy is the identity
+    grid[0:3, :, :] = fo.PML()
+    obj = fo.Object(permittivity=2.0)
+    grid[5:8, 3:7, 0:1] = obj
+    obj.inverse_permittivity = np.repeat(design[..., None], 3, axis=-1)
+    grid[9, 5, 0] = fo.PointSource(period=8)
+    grid[:, 5, 0] = fo.LineDetector()
+    return grid, obj
+
+
+def test_periodic_one_plane_axis_transposes_to_identity():
+    """A periodic boundary on an axis of one plane copies each value onto
+    itself; its transpose must leave the adjoint alone (not move and zero it).
+    Checked against central differences of the forward."""
+    steps = 14
+    rng = np.random.default_rng(3)
+    design = rng.uniform(0.4, 0.9, size=(3, 4, 1))
+
+    def loss_of(d):
+        grid, obj = _plane_periodic_scene(d)
+        recs, curls = fa.forward_records(grid, steps, obj)
+        name = next(iter(recs))
+        e = torch.tensor(recs[name]["E"], requires_grad=True)
+        loss = (e ** 2).sum()
+        return loss, e, grid, obj, curls, name
+
+    loss, e, grid, obj, curls, name = loss_of(design)
+    loss.backward()
+    seeds = {name: {"E": e.grad.numpy(), "H": None}}
+    grad = fa.adjoint_gradient(grid, steps, obj, 0, seeds, curls).sum(axis=-1)
+    h = 1e-6
+    for idx in [(0, 0, 0), (1, 2, 0), (2, 3, 0)]:
+        dp, dm = design.copy(), design.copy()
+        dp[idx] += h
+        dm[idx] -= h
+        fd = (float(loss_of(dp)[0]) - float(loss_of(dm)[0])) / (2 * h)
+        assert abs(fd - grad[idx]) <= 1e-6 * max(1.0, abs(fd)), (idx, fd, grad[idx])

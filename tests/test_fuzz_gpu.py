@@ -10,6 +10,8 @@ rows, x chunk, material copies).  float64 must match the oracle to 1e-12 relativ
 to 1e-4, on E, H and every detector trace.
 """
 
+import os
+
 import numpy as np
 import pytest
 
@@ -104,7 +106,8 @@ def random_tuning(seed, nz, precision):
     return tune
 
 
-SEEDS = list(range(40))
+# FDTD_FUZZ_SEEDS widens the sweep (e.g. 400 for a longer soak)
+SEEDS = list(range(int(os.environ.get("FDTD_FUZZ_SEEDS", "40"))))
 
 
 @pytest.mark.parametrize("precision", ["float64", "float32"])
