@@ -7,7 +7,7 @@ periodic boundaries on random axes in a random registration order, up to
 three overlapping objects of all kinds, point, line and plane sources,
 line/block/plane detectors, and a plan choice (kernel variant, PML mode, tile
 rows, x chunk, material copies).  float64 must match the oracle to 1e-12 relative L2, float32
-to 1e-4, on E, H and every detector trace.
+and compensated float32 to 1e-4, on E, H and every detector trace.
 """
 
 import os
@@ -110,7 +110,7 @@ def random_tuning(seed, nz, precision):
 SEEDS = list(range(int(os.environ.get("FDTD_FUZZ_SEEDS", "40"))))
 
 
-@pytest.mark.parametrize("precision", ["float64", "float32"])
+@pytest.mark.parametrize("precision", ["float64", "float32", "float32c"])
 @pytest.mark.parametrize("seed", SEEDS)
 def test_random_scene_matches_oracle(fd, seed, precision):
     fd.set_backend("gb300." + precision)
