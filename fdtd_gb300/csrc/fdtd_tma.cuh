@@ -1,17 +1,22 @@
 // TMA-staged fused half steps.
 //
-// A CTA of 32 x TY threads owns a tile of TY rows (y) by 32*V cells (z) and
-// marches along x over a chunk of planes.  Each field is viewed as a 2D
-// tensor of (nx*ny) rows by 3*nz values (8-byte elements for the tensor map)
-// and one TMA load per field and plane fills a shared-memory stage:
+// A CTA of TZ x TY threads (32 x 8, 32 x 4 or 16 x 16) owns a tile of TY rows
+// (y) by TZ*V cells (z) and marches along x over a chunk of planes.  Each
+// field is viewed as a 2D tensor of (nx*ny) rows by 3*nz values (8-byte
+// elements for the tensor map) and one TMA load per field and plane fills a
+// shared-memory stage:
 //
 //   E half: H tile of TY+1 rows (row 0 = j0-1) with a 4-value prefix that
 //           holds the cell k0-1, plus the E, inverse-permittivity (and
 //           compensation) tiles of TY rows;
 //   H half: E tile of TY+1 rows (row TY = j0+TY) with a 4-value suffix that
-//           holds the cell k0+32V, plus the H, inverse-permeability (and
+//           holds the cell k0+TZ*V, plus the H, inverse-permeability (and
 //           compensation) tiles.  Plane i needs E(i) and E(i+1), so two
 //           stages are read at once.
+//
+// The material tile is the three values per cell, a one-byte index per cell
+// into a table staged in shared memory at kernel start (a uint8 tensor map
+// of (nx*ny) rows by nz bytes), or absent for a uniform material (MAT).
 //
 // A ring of S stages keeps S-1 planes of loads in flight while the threads
 // compute from shared memory; the E half keeps H(i-1) in registers.  The
