@@ -41,6 +41,26 @@ static int validate(const Plan &p, const fdtd_adjoint_args *a) {
     return FDTD_OK;
 }
 
+// One transposed slab kernel: one thread per cell with 32-bit cell indices
+// below 2^31 cells, else a grid-stride loop with 64-bit indices.
+template <class T, bool IS_E, int A>
+static void launch_adj_slab_axis(const GridK &g, const AdjAux &x, int slab, long cells, cudaStream_t st) {
+    if (cells < (1L << 31)) {
+        const unsigned blocks = (unsigned)((cells + kThreads - 1) / kThreads);
+        k_adj_slab<T, IS_E, A, uint32_t><<<blocks > 0 ? blocks : 1, kThreads, 0, st>>>(g, x, slab);
+    } else {
+        k_adj_slab<T, IS_E, A, uint64_t><<<grid_stride_blocks(cells), kThreads, 0, st>>>(g, x, slab);
+    }
+}
+
+template <class T, bool IS_E>
+static void launch_adj_slab(const GridK &g, const AdjAux &x, int slab, long cells, cudaStream_t st) {
+    const int a = g.slab[slab].axis;
+    if (a == 0) launch_adj_slab_axis<T, IS_E, 0>(g, x, slab, cells, st);
+    else if (a == 1) launch_adj_slab_axis<T, IS_E, 1>(g, x, slab, cells, st);
+    else launch_adj_slab_axis<T, IS_E, 2>(g, x, slab, cells, st);
+}
+
 template <class T, int V>
 static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
     GridK g = p.k;
@@ -97,7 +117,7 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
         k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
         if (p.pml_split)
             for (int q = 0; q < g.nslab; ++q)
-                k_adj_slab<T, false><<<grid_stride_blocks(slab_cells(g.slab[q])), kThreads, 0, st>>>(g, x, q);
+                launch_adj_slab<T, false>(g, x, q, slab_cells(g.slab[q]), st);
 
         // transposed E half
         if (a->seed_E && p.n_probe)
@@ -132,7 +152,7 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
         k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
         if (p.pml_split)
             for (int q = 0; q < g.nslab; ++q)
-                k_adj_slab<T, true><<<grid_stride_blocks(slab_cells(g.slab[q])), kThreads, 0, st>>>(g, x, q);
+                launch_adj_slab<T, true>(g, x, q, slab_cells(g.slab[q]), st);
         for (int q = p.n_objects - 1; q >= 0; --q) {
             const ItemK &o = p.items_host[q];
             const long reach = (long)(o.hi[0] - std::max(0, o.lo[0] - 1)) * (o.hi[1] - std::max(0, o.lo[1] - 1)) *

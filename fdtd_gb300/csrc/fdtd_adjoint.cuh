@@ -348,12 +348,15 @@ __global__ void __launch_bounds__(kThreads) k_adj_E(const GridK g, const AdjAux 
 // transposed E half: lam_H and the E-side adjoint auxiliaries, after k_adj_E)
 // or adj_slab_H (lam_E and the H-side ones, after k_adj_H).  The kernel reads
 // the adjoint field it does not write, and the current auxiliary buffer.
-template <class T, bool IS_E>
+// The slab normal A is a template parameter and the cell index type I is
+// 32-bit whenever the slab has fewer than 2^31 cells (no 64-bit divisions).
+template <class T, bool IS_E, int A, class I>
 __global__ void __launch_bounds__(kThreads) k_adj_slab(const GridK g, const AdjAux x, int s) {
     const SlabK &S = g.slab[s];
-    const int a = S.axis, th = S.th;
-    const int n0 = a == 0 ? th : g.nx, n1 = a == 1 ? th : g.ny, n2 = a == 2 ? th : g.nz;
-    const long total = (long)n0 * n1 * n2;
+    constexpr int a = A;
+    const int th = S.th;
+    const int n1 = a == 1 ? th : g.ny, n2 = a == 2 ? th : g.nz;
+    const I total = (I)(a == 0 ? th : g.nx) * (I)n1 * (I)n2;
     const T c = material_courant<T>(g);  // courant * material factor
     const T *L = (const T *)(IS_E ? g.E : g.H);  // lam_E (E half) or lam_H (H half), read
     T *O = (T *)(IS_E ? g.H : g.E);              // the adjoint field updated
@@ -363,12 +366,13 @@ __global__ void __launch_bounds__(kThreads) k_adj_slab(const GridK g, const AdjA
     const T *__restrict__ bt = (const T *)(IS_E ? S.bE : S.bH);
     const T *__restrict__ ct = (const T *)(IS_E ? S.cE : S.cH);
     const T f = s < g.nslab_fused ? T(1) : T(0);
-    const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+    constexpr int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
     // one step along the normal, in cells and in auxiliary pairs (same count)
     const long cstride = a == 0 ? (long)g.ny * g.nz : (a == 1 ? (long)g.nz : 1L);
     const long pstride = cstride;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const int i0 = (int)(t / ((long)n1 * n2)), i1 = (int)((t / n2) % n1), i2 = (int)(t % n2);
+    for (I t = (I)blockIdx.x * (I)blockDim.x + threadIdx.x; t < total; t += (I)gridDim.x * (I)blockDim.x) {
+        const I r = t / (I)n2;
+        const int i2 = (int)(t - r * (I)n2), i1 = (int)(r % (I)n1), i0 = (int)(r / (I)n1);
         const int l = a == 0 ? i0 : (a == 1 ? i1 : i2);
         const int gi = a == 0 ? i0 + S.start : i0, gj = a == 1 ? i1 + S.start : i1, gk = a == 2 ? i2 + S.start : i2;
         const size_t cell = ((size_t)gi * g.ny + gj) * g.nz + gk;
