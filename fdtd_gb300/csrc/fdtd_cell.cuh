@@ -86,11 +86,11 @@ __device__ __forceinline__ bool aligned16_ptr(const void *p) { return ((uintptr_
 
 // Objects of a thread's V cells (fdtd/objects.py:92-129, 198-221, 256-269),
 // items in list order; each cell gets the same operations in the same order
-// as one at a time.  Where all V cells lie in a box and their coefficients
-// start on a 16-byte boundary they are read with 16-byte loads: one 4- or
-// 8-byte load per value at a 3- or 9-value stride touches a sector per lane,
-// and the CTAs holding a 1.6 % anisotropic box (config 5) took twice as long
-// per plane as the others.
+// as one at a time.  In float32, where all V cells lie in a box and their
+// coefficients start on a 16-byte boundary, they are read with 16-byte
+// loads: one 4-byte load per value at a 3- or 9-value stride touches a sector
+// per lane, and the CTAs holding a 1.6 % anisotropic box (config 5) took
+// twice as long per plane as the others.
 template <class P, int V>
 __device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, int k0, typename P::T c,
                                                 const typename P::T (&cu)[3][V], typename P::T (&e)[3 * V],
@@ -100,7 +100,10 @@ __device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, in
         const ItemK &o = g.items[g.obj_idx[it]];
         if (i < o.lo[0] || i >= o.hi[0] || j < o.lo[1] || j >= o.hi[1] || k0 >= o.hi[2] || k0 + V <= o.lo[2])
             continue;
-        if constexpr (V > 1) {
+        // float32 only: in float64 the values held for the wide loads pushed
+        // the staged E pass past 128 registers (one CTA per SM instead of
+        // two: config 3 float64 15.3 -> 14.0 Gcell/s)
+        if constexpr (V > 1 && sizeof(T) == 4) {
             const size_t li = k0 >= o.lo[2] ? box_index(o, i, j, k0) : 0;
             const bool whole = k0 >= o.lo[2] && k0 + V <= o.hi[2];
             if (whole && o.kind == FDTD_ITEM_ANISOTROPIC) {
