@@ -320,7 +320,7 @@ def cpu_oracle_rate(budget_s, n_full):
     for _ in range(steps):
         g.step()
     dt = time.perf_counter() - t0
-    return {"value": n ** 3 * steps / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": n ** 3 * steps / dt / 1e9, "unit": UNIT, "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
             "sample": f"numpy float64 oracle of fdtd's time step on the config-3 generator cropped to {n}^3 "
                       f"(3-cell PML, periodic x, point source, line detector), {steps} steps, "
                       f"{dt:.1f} s, one host core (numpy elementwise is single-threaded)"}
@@ -563,7 +563,8 @@ def reference_arm(args):
         "data": "synthetic: config-3 generator (seed 3), zero initial fields",
         "config": {"workload": f"config3_{args.n}^3_float32", "sample_grid": [n, n, n],
                    "parallelism": "single host process"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
