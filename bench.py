@@ -62,7 +62,11 @@ def parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
-    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--impl", choices=["gb300", "reference", "reference-gpu"], default="gb300",
+                   help="reference: the reference's numpy time step on the host cores (restated); "
+                        "reference-gpu: the reference's own torch CUDA backend from baseline/_ref")
+    p.add_argument("--ref-backend", default="torch.cuda.float64",
+                   help="backend name of the reference for --impl reference-gpu")
     p.add_argument("--n", type=int, default=768, help="grid edge (config 3 is 768)")
     p.add_argument("--pml", type=int, default=-1, help="PML cells on y and z (default 20 scaled by n/768; 0 = none)")
     p.add_argument("--x-chunk", type=int, default=0, help="planes per CTA along x (0 = plan default)")
@@ -570,10 +574,58 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def reference_gpu_arm(args):
+    """The reference's own GPU path (its torch CUDA backend: one PyTorch
+    elementwise kernel per operation, about 490 launches per step) on the same
+    config-3 grid, from the unmodified package installed in baseline/_ref
+    (with the no-op matplotlib stand-in of tests/golden/mplstub).  A comparison
+    figure for the GPU arm, not the CPU baseline of the contract."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    ref_dir = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isfile(os.path.join(ref_dir, "fdtd", "__init__.py")):
+        print(json.dumps({"impl": "reference-gpu", "unavailable": "reference not installed in baseline/_ref"}))
+        return
+    sys.path[:0] = [ref_dir, os.path.join(ROOT, "tests", "golden", "mplstub")]
+    import torch
+
+    import fdtd as ref
+    from fdtd_gb300 import scenes
+
+    ref.set_backend(args.ref_backend)
+    n = args.n
+    pml = max(2, int(round(20 * n / 768))) if args.pml < 0 else args.pml
+    g = scenes.c3(ref, n=n, pml=pml, eps=scenes.c3_permittivity(n), detector=True)
+    g.run(args.warmup, progress_bar=False)
+    on_gpu = "cuda" in args.ref_backend
+    if on_gpu:
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        g.run(args.steps, progress_bar=False)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+    else:
+        t0 = time.perf_counter()
+        g.run(args.steps, progress_bar=False)
+        ms = (time.perf_counter() - t0) * 1e3
+    print(json.dumps({
+        "impl": "reference-gpu", "metric": METRIC, "value": n ** 3 * args.steps / (ms * 1e-3) / 1e9, "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "backend": args.ref_backend, "data": "synthetic: config-3 generator (seed 3)",
+        "config": {"workload": f"config3_{n}^3", "grid": [n, n, n], "pml": pml},
+        "threads": None if on_gpu else torch.get_num_threads(),
+        "peak_memory_gb": torch.cuda.max_memory_allocated() / 1e9 if on_gpu else None}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.impl == "reference-gpu":
+        reference_gpu_arm(args)
     elif args.adjoint_only:
         import fdtd_gb300 as fd
         from fdtd_gb300 import scenes
