@@ -578,7 +578,8 @@ def reference_gpu_arm(args):
     """The reference's own GPU path (its torch CUDA backend: one PyTorch
     elementwise kernel per operation, about 490 launches per step) on the same
     config-3 grid, from the unmodified package installed in baseline/_ref
-    (with the no-op matplotlib stand-in of tests/golden/mplstub).  A comparison
+    (with the no-op matplotlib stand-in of tests/golden/mplstub, and of
+    tests/golden/tqdmstub where tqdm is not installed).  A comparison
     figure for the GPU arm, not the CPU baseline of the contract."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -588,6 +589,7 @@ def reference_gpu_arm(args):
         print(json.dumps({"impl": "reference-gpu", "unavailable": "reference not installed in baseline/_ref"}))
         return
     sys.path[:0] = [ref_dir, os.path.join(ROOT, "tests", "golden", "mplstub")]
+    sys.path.append(os.path.join(ROOT, "tests", "golden", "tqdmstub"))  # only if tqdm is absent
     import torch
 
     import fdtd as ref
