@@ -84,5 +84,5 @@ def test_periodic_one_plane_axis_transposes_to_identity():
         dp, dm = design.copy(), design.copy()
         dp[idx] += h
         dm[idx] -= h
-        fd = (float(loss_of(dp)[0]) - float(loss_of(dm)[0])) / (2 * h)
+        fd = (float(loss_of(dp)[0].detach()) - float(loss_of(dm)[0].detach())) / (2 * h)
         assert abs(fd - grad[idx]) <= 1e-6 * max(1.0, abs(fd)), (idx, fd, grad[idx])
