@@ -87,6 +87,28 @@ def test_float32_close_to_reference_golden(fd, prec, name):
     _compare(golden_scenes.snapshot(grid), ref, TOL32, f"{name}/{prec}")
 
 
+STAGED_PLANS = [dict(variant=2, pml_mode=1), dict(variant=2, pml_mode=2), dict(variant=2, pml_mode=3)]
+
+
+@pytest.mark.parametrize("tune", STAGED_PLANS, ids=lambda t: f"pml{t['pml_mode']}")
+@pytest.mark.parametrize("prec", ["float64", "float32"])
+@pytest.mark.parametrize("name", ["c1", "c3_periodic_first", "c3_periodic_last"])
+def test_staged_compact_plans_against_reference_golden(fd, prec, name, tune):
+    """The TMA-staged passes reading compact material copies (one-byte
+    indices; these scenes have a few permittivity values and nz = 16), with
+    the PML slabs fused, split, or partly kept, against the fixtures the
+    reference itself made."""
+    fd.set_backend("gb300." + prec)
+    grid, steps, drive = golden_scenes.SCENES[name](fd)
+    eng = grid._ensure_engine()
+    eng.set_tuning(**tune)
+    assert eng.tiling()["variant"] == 2 and eng.compact_materials()[0] is not None
+    drive(grid, steps)
+    eng.check_status()
+    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    _compare(golden_scenes.snapshot(grid), ref, TOL64 if prec == "float64" else TOL32, f"{name}/{prec}/{tune}")
+
+
 def _curl_via_abi(native, fn, arr, precision, dtype):
     t = torch.as_tensor(arr, dtype=dtype, device="cuda").contiguous()
     out = torch.empty_like(t)
