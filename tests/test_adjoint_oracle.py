@@ -86,3 +86,41 @@ def test_periodic_one_plane_axis_transposes_to_identity():
         dm[idx] -= h
         fd = (float(loss_of(dp)[0].detach()) - float(loss_of(dm)[0].detach())) / (2 * h)
         assert abs(fd - grad[idx]) <= 1e-6 * max(1.0, abs(fd)), (idx, fd, grad[idx])
+
+
+@pytest.mark.parametrize("seed", [0, 3, 10, 13, 35, 114])
+def test_adjoint_oracle_matches_central_differences_on_random_scenes(seed):
+    """The adjoint oracle on the random scenes of the GPU adjoint fuzz test
+    (random boundaries, objects, sources, detectors, design kind) against
+    central differences of the oracle's own forward loss at three design
+    entries."""
+    import test_adjoint_fuzz_gpu as fz
+
+    steps = fz.STEPS
+
+    def run(value):
+        grid, design, _, weights, _, _ = fz.adjoint_scene(fo, seed)
+        design.inverse_permittivity = value if value.ndim == 5 else np.repeat(value[..., None], 3, axis=-1)
+        recs, curls = fa.forward_records(grid, steps, design)
+        outs = {name: {f: torch.tensor(v, requires_grad=True) for f, v in r.items()} for name, r in recs.items()}
+        return fz.loss_of(outs, weights), outs, grid, design, curls
+
+    _, _, value, _, _, _ = fz.adjoint_scene(fo, seed)
+    loss, outs, grid, design, curls = run(value)
+    loss.backward()
+    seeds = {name: {f: (None if t.grad is None else t.grad.numpy()) for f, t in r.items()}
+             for name, r in outs.items()}
+    grad = fa.adjoint_gradient(grid, steps, design, 0, seeds, curls)
+    if value.ndim == 3:
+        grad = grad.sum(axis=-1)
+    rng = np.random.default_rng(seed + 77)
+    h = 1e-6
+    for _ in range(3):
+        idx = tuple(int(rng.integers(0, m)) for m in value.shape)
+        vp, vm = value.copy(), value.copy()
+        vp[idx] += h
+        vm[idx] -= h
+        fd = (float(run(vp)[0].detach()) - float(run(vm)[0].detach())) / (2 * h)
+        # central differences: truncation ~h^2, rounding ~eps*|loss|/h
+        noise = 1e-9 * max(1.0, abs(float(loss.detach())))
+        assert abs(fd - grad[idx]) <= 1e-5 * abs(fd) + noise, (seed, idx, fd, grad[idx])
