@@ -12,6 +12,8 @@ The reference imports matplotlib for plotting only; a no-op stand-in from
   ``RandomState(0).randn(3,3,3,3)`` and ``RandomState(1).randn(3,3,3,3)``).
 * ``ref_<scene>.npz`` -- final E, H and every detector trace for each scene of
   ``golden_scenes.SCENES`` after its stated number of steps.
+* ``ref_fuzz.npz`` -- the same for the first random forward scenes of
+  ``tests/test_fuzz_gpu.py`` (scene argument ``fuzz``).
 """
 
 import os
@@ -48,6 +50,28 @@ def fourier_fixture(fdtd, grid):
                 arr=arr, arr_freqs=np.asarray(f_a), arr_fft=np.asarray(s_a))
 
 
+FUZZ_SEEDS = list(range(12))
+FUZZ_STEPS = 15
+
+
+def fuzz_fixture(fdtd):
+    """Final E, H and every detector trace of the random forward scenes of
+    tests/test_fuzz_gpu.py (without their PlaneDetector) after FUZZ_STEPS."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from test_fuzz_gpu import random_scene
+
+    out = {"seeds": np.array(FUZZ_SEEDS), "steps": np.array(FUZZ_STEPS)}
+    for seed in FUZZ_SEEDS:
+        grid = random_scene(fdtd, seed, plane_detector=False)
+        grid.run(FUZZ_STEPS, progress_bar=False)
+        out[f"s{seed}_E"] = np.asarray(grid.E)
+        out[f"s{seed}_H"] = np.asarray(grid.H)
+        for i, d in enumerate(grid.detectors):
+            out[f"s{seed}_d{i}_E"] = np.array(d.E)
+            out[f"s{seed}_d{i}_H"] = np.array(d.H)
+    return out
+
+
 def main(ref_path, only=None):
     fdtd = load_reference(ref_path)
     sys.path.insert(0, REPO)
@@ -59,6 +83,9 @@ def main(ref_path, only=None):
     H1 = np.random.RandomState(1).randn(3, 3, 3, 3)
     np.savez(os.path.join(HERE, "ref_curls.npz"), E=E0, curl_E=curl_E(E0), H=H1, curl_H=curl_H(H1),
              reference_version=fdtd.__version__)
+    if not only or "fuzz" in only:
+        np.savez_compressed(os.path.join(HERE, "ref_fuzz.npz"), **fuzz_fixture(fdtd))
+        print("fuzz", len(FUZZ_SEEDS), "seeds")
     for name, build in golden_scenes.SCENES.items():
         if only and name not in only:
             continue

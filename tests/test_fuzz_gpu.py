@@ -21,7 +21,9 @@ from oracle import fdtd_oracle as fo
 pytestmark = pytest.mark.gpu
 
 
-def random_scene(mod, seed):
+def random_scene(mod, seed, plane_detector=True):
+    """The scene of a seed; without the PlaneDetector (not a reference
+    component) it also builds on the reference package."""
     rng = np.random.default_rng(seed)
     side = np.random.default_rng(seed + 2000)  # draws added later, kept off the main stream
     nz = int(rng.choice([1, 7, 8, 12, 13, 16]))
@@ -90,7 +92,8 @@ def random_scene(mod, seed):
     grid[:, p[1], p[2]] = mod.LineDetector()
     b0 = [int(rng.integers(0, max(1, m - 2))) for m in n]
     grid[b0[0]:b0[0] + 1, b0[1]:b0[1] + 1, b0[2]:b0[2] + (1 if nz > 1 else 0)] = mod.BlockDetector()
-    grid[:, :, int(rng.integers(0, nz))] = mod.PlaneDetector()
+    if plane_detector:
+        grid[:, :, int(rng.integers(0, nz))] = mod.PlaneDetector()
     return grid
 
 

@@ -75,3 +75,37 @@ def test_gaussian_plane_source_envelope():
     peak = np.argmax(np.abs(vals))
     assert abs(peak * g.time_step - src.center_s) < 2 * src.period_s
     assert abs(vals[0]) < 1e-3
+
+
+def _fuzz_fixture():
+    return np.load(os.path.join(GOLDEN, "ref_fuzz.npz"))
+
+
+@pytest.mark.parametrize("seed", list(range(12)))
+def test_oracle_matches_reference_on_random_scenes(seed):
+    """The random forward scenes of the GPU fuzz test (less their
+    PlaneDetector), run by the reference itself (tests/golden/make_golden.py):
+    the oracle the GPU fuzz compares against reproduces them bit for bit, or
+    to 1e-14 where an anisotropic object's 3x3 product is summed in another
+    order than numpy's einsum."""
+    import test_fuzz_gpu
+
+    ref = _fuzz_fixture()
+    assert seed in ref["seeds"]
+    grid = test_fuzz_gpu.random_scene(fo, seed, plane_detector=False)
+    grid.run(int(ref["steps"]))
+    aniso = any(isinstance(o, fo.AnisotropicObject) for o in grid.objects)
+    got = {f"s{seed}_E": grid.E, f"s{seed}_H": grid.H}
+    for i, d in enumerate(grid.detectors):
+        got[f"s{seed}_d{i}_E"] = np.array(d.E)
+        got[f"s{seed}_d{i}_H"] = np.array(d.H)
+    keys = [k for k in ref.files if k.startswith(f"s{seed}_")]
+    assert sorted(keys) == sorted(got)
+    for k in keys:
+        a, b = np.asarray(got[k], dtype=np.float64), ref[k]
+        assert a.shape == b.shape, k
+        if aniso:
+            scale = max(np.linalg.norm(b), 1e-300)
+            assert np.linalg.norm(a - b) <= 1e-14 * scale, k
+        else:
+            assert np.array_equal(a, b), k
