@@ -16,14 +16,16 @@ fdtd/grid.py:275-325), applied in reverse order:
 * PML auxiliaries and corrections (fdtd/boundaries.py:409-487, compact
   storage of ``fdtd_oracle.PML``);
 * periodic copies (fdtd/boundaries.py:184-219): F[dst] = F[src] transposes to
-  lam[src] += lam[dst], lam[dst] = 0;
+  lam[src] += lam[dst], lam[dst] = 0 (on an axis of one plane the copy and its
+  transpose are the identity);
 * objects (fdtd/objects.py:118-277), including the gradient with respect to a
   design object's inverse permittivity;
 * hard sources (fdtd/sources.py:476-486) zero the adjoint at their cells; soft
   sources do nothing;
 * detector samples add the loss gradient (the seeds).
 
-``tests/test_adjoint_oracle.py`` pins this restatement to the fixtures.
+``tests/test_adjoint_oracle.py`` pins this restatement to the fixtures and to
+central differences of the oracle forward on random scenes.
 """
 
 import numpy as np
