@@ -10,9 +10,15 @@
   grid precision, grown geometrically; detectors view their slice of it;
 * DFT phases -- (n, n_freq_total, 2) float64 (cos, -sin) per step.
 
+* compact material copies -- for the staged passes, a table of the distinct
+  inverse-material value triples and a one-byte index per cell (or one triple
+  for a uniform material), kept in step with in-place changes of the
+  material arrays (``compact_material``).
+
 The plan is rebuilt when components are registered, when an object's
-coefficients change, or when the tiling option changes; detector records
-taken before a rebuild are kept (copied out of the old buffer).
+coefficients change, when the compact copies change layout, or when the
+tiling option changes; detector records taken before a rebuild are kept
+(copied out of the old buffer).
 """
 
 import ctypes
