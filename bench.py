@@ -73,7 +73,9 @@ def parse():
     p.add_argument("--variant", type=int, default=0, help="0 auto, 1 register streaming, 2 TMA-staged")
     p.add_argument("--tile-rows", type=int, default=0)
     p.add_argument("--stages", type=int, default=0)
-    p.add_argument("--pml-mode", type=int, default=0, help="0 auto, 1 PML inside the fused pass, 2 slab kernels")
+    p.add_argument("--pml-mode", type=int, default=0,
+                   help="0 auto, 1 PML inside the fused pass, 2 slab kernels, 3 leading x/y slabs fused and the "
+                        "rest in slab kernels")
     p.add_argument("--materials", type=int, default=0,
                    help="0 compact material copies where possible (one-byte index or uniform), 1 full arrays")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
