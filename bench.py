@@ -321,7 +321,7 @@ def cpu_oracle_rate(budget_s, n_full):
     t0 = time.perf_counter()
     g.step()
     per = time.perf_counter() - t0
-    steps = int(max(3, min(60, budget_s / max(per, 1e-3))))
+    steps = int(max(3, min(2000, budget_s / max(per, 1e-3))))
     t0 = time.perf_counter()
     for _ in range(steps):
         g.step()
