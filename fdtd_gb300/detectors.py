@@ -271,6 +271,21 @@ class CurrentDetector(_Detector):
         return np.meshgrid(np.asarray(self.x, np.int64), np.asarray(self.y, np.int64),
                            np.asarray(self.z, np.int64), indexing="ij")
 
+    def single_point_current(self, px, py, pz):
+        """The current around the z edge at (px, py, pz) from the grid's
+        present H (fdtd/detectors.py:404-464), with the reference's operation
+        order, its running sum of the second y term and Python's wrap-around of
+        index -1; a 0-d tensor.  The time step computes the same on the
+        device for every point of the detector."""
+        H, du = self.grid.H, self.grid.grid_spacing
+        cv1 = (H[px, py - 1, pz, 0] - H[px, py, pz, 0]) * du
+        cv2 = (H[px, py, pz, 1] - H[px - 1, py, pz, 1]) * du
+        c1 = cv1 + cv2
+        cv1 = (H[px, py - 1, pz - 1, 0] - H[px, py, pz - 1, 0]) * du
+        cv2 = cv2 + (H[px, py, pz - 1, 1] - H[px - 1, py, pz - 1, 1]) * du
+        c2 = cv1 + cv2
+        return (c1 + c2) / 2.0
+
     def detector_values(self):
         """Outputs of the detector, {'I': records}."""
         return {"I": self.I}

@@ -20,6 +20,11 @@ from . import constants as const
 from .backend import backend as bd
 
 
+
+# the per-component hooks the reference's Grid calls every half step
+# (fdtd/grid.py:275-325); the fused time step replaces them
+_STEP_HOOKS = ("update_phi_E", "update_phi_H", "update_E", "update_H", "detect_E", "detect_H")
+
 class Grid:
     """The FDTD grid: fields, materials and the registered components."""
 
@@ -195,6 +200,12 @@ class Grid:
             x, y, z = key
         else:
             raise KeyError("maximum number of indices for the grid is 3")
+        hooks = [h for h in _STEP_HOOKS if callable(getattr(attr, h, None))]
+        if hooks:
+            # a component (e.g. a user subclass) that brings its own per-step
+            # hooks cannot run inside the fused time step
+            raise NotImplementedError(f"{type(attr).__name__} defines the per-step hook(s) {', '.join(hooks)}; "
+                                      "the gb300 backend fuses the time step and does not call component hooks")
         attr._register_grid(grid=self, x=self._handle_single_key(x), y=self._handle_single_key(y),
                             z=self._handle_single_key(z))
 

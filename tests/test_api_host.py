@@ -221,3 +221,42 @@ def test_soft_arbitrary_point_source_registration(grid, fd):
     grid[2:4, 3:5, 7] = cd  # inclusive ranges like BlockDetector
     assert (cd.x, cd.y, cd.z) == ([2, 3, 4], [3, 4, 5], [7]) and not hasattr(cd, "E")
     assert cd.detector_values()["I"] is cd.I
+
+
+def test_single_point_current_matches_oracle(fd):
+    """CurrentDetector.single_point_current (fdtd/detectors.py:404-464) on the
+    grid's present H, against the oracle's restatement, including the index
+    wrap at the grid's first planes."""
+    fd.set_backend("gb300.float64")
+    g = fd.Grid((6, 5, 4), grid_spacing=100e-9)
+    o = fo.Grid((6, 5, 4), grid_spacing=100e-9)
+    det, odet = fd.CurrentDetector(), fo.CurrentDetector()
+    g[2, 2, 2] = det
+    o[2, 2, 2] = odet
+    h = np.random.default_rng(5).standard_normal((6, 5, 4, 3))
+    g.H[...] = torch.as_tensor(h, device=g.H.device)
+    o.H[...] = h
+    for p in [(2, 2, 2), (0, 0, 0), (5, 4, 3), (0, 3, 1)]:
+        assert float(det.single_point_current(*p)) == float(odet._point(*p))
+
+
+def test_components_with_step_hooks_are_refused(grid, fd):
+    """The reference's Grid calls update_E/update_H/update_phi_*/detect_*
+    hooks of its components every half step; a component that brings such a
+    hook (a user subclass) cannot run inside the fused time step, so
+    registering it raises NotImplementedError instead of ignoring the hook."""
+
+    class MySource(fd.PointSource):
+        def update_E(self):
+            pass
+
+    class MyDetector(fd.LineDetector):
+        def detect_H(self):
+            pass
+
+    with pytest.raises(NotImplementedError):
+        grid[4, 4, 4] = MySource(period=10)
+    with pytest.raises(NotImplementedError):
+        grid[:, 4, 4] = MyDetector()
+    assert grid.sources == [] and grid.detectors == []
+    grid[4, 4, 4] = fd.PointSource(period=10)  # the package's own components carry no hooks
