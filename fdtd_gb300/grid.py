@@ -297,6 +297,21 @@ class Grid:
         return s
 
     # --- detector export (fdtd/grid.py:407-439, 490-514) -----------------------
+    # --- plotting and complex fields: not part of this backend ------------------
+    def visualize(self, *args, **kwargs):
+        """fdtd/visualization.py:28-336 plots with matplotlib; this backend has no
+        plotting (copy grid.E / grid.H to the host and plot them there)."""
+        raise NotImplementedError("visualize is not part of the gb300 backend (no plotting)")
+
+    def generate_video(self, *args, **kwargs):
+        """fdtd/grid.py:441-488 calls ffmpeg on plotted frames; not part of this backend."""
+        raise NotImplementedError("generate_video is not part of the gb300 backend (no plotting)")
+
+    def promote_dtypes_to_complex(self):
+        """fdtd/grid.py:353-356: complex fields are not supported (and broken in
+        the reference's boundaries, fdtd/boundaries.py:106-116)."""
+        raise NotImplementedError("complex fields are not supported by the gb300 backend")
+
     def save_simulation(self, sim_name=None):
         """Create ``fdtd_output/fdtd_output_<timestamp> (<sim_name>)`` and remember it."""
         os.makedirs("fdtd_output", exist_ok=True)

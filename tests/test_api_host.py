@@ -260,3 +260,11 @@ def test_components_with_step_hooks_are_refused(grid, fd):
         grid[:, 4, 4] = MyDetector()
     assert grid.sources == [] and grid.detectors == []
     grid[4, 4, 4] = fd.PointSource(period=10)  # the package's own components carry no hooks
+
+
+def test_plotting_and_complex_raise(grid):
+    """Plotting (fdtd/visualization.py) and complex fields are outside this
+    backend: the reference's method names exist and raise NotImplementedError."""
+    for call in (grid.visualize, grid.generate_video, grid.promote_dtypes_to_complex):
+        with pytest.raises(NotImplementedError):
+            call()
