@@ -25,12 +25,13 @@ from .fourier import FrequencyRoutines
 from .grid import Grid
 from .objects import AbsorbingObject, AnisotropicObject, Object
 from .sources import GaussianPlaneSource, LineSource, PlaneSource, PointSource, SoftArbitraryPointSource
-from . import adjoint, constants, waveforms, conversions
+from . import adjoint, constants, waveforms, conversions, visualization
+from .visualization import dB_map_2D, plot_detection
 
 __all__ = [
     "Grid", "PML", "PeriodicBoundary", "DomainBorderPML", "Object", "AbsorbingObject",
     "AnisotropicObject", "PointSource", "LineSource", "PlaneSource", "GaussianPlaneSource",
     "SoftArbitraryPointSource", "LineDetector", "BlockDetector", "CurrentDetector", "PlaneDetector",
     "DFTPlaneDetector", "FrequencyRoutines", "backend", "set_backend", "adjoint", "constants", "waveforms",
-    "conversions",
+    "conversions", "visualization", "dB_map_2D", "plot_detection",
 ]

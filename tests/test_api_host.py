@@ -268,3 +268,9 @@ def test_plotting_and_complex_raise(grid):
     for call in (grid.visualize, grid.generate_video, grid.promote_dtypes_to_complex):
         with pytest.raises(NotImplementedError):
             call()
+
+
+def test_plotting_helpers_raise(fd):
+    for fn in (fd.dB_map_2D, fd.plot_detection, fd.visualization.visualize):
+        with pytest.raises(NotImplementedError):
+            fn()
