@@ -19,11 +19,45 @@ import torch
 from . import constants as const
 from .backend import backend as bd
 
-
-
 # the per-component hooks the reference's Grid calls every half step
 # (fdtd/grid.py:275-325); the fused time step replaces them
 _STEP_HOOKS = ("update_phi_E", "update_phi_H", "update_E", "update_H", "detect_E", "detect_H")
+
+
+def _curl(name, F):
+    """A stand-alone curl through the C ABI (fdtd_curl_E / fdtd_curl_H) on the
+    current CUDA stream; float32 stays float32, anything else runs in float64."""
+    from . import _native
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("the gb300 backend needs a CUDA device; this machine has none")
+    t = torch.as_tensor(F)
+    if t.dtype != torch.float32:
+        t = t.to(torch.float64)
+    if t.dim() != 4 or t.shape[-1] != 3:
+        raise ValueError("the field must have the shape (Nx, Ny, Nz, 3)")
+    t = t.to("cuda").contiguous()
+    out = torch.empty_like(t)
+    precision = _native.FLOAT32 if t.dtype == torch.float32 else _native.FLOAT64
+    stream = torch.cuda.current_stream(t.device).cuda_stream
+    nx, ny, nz, _ = t.shape
+    _native.check(getattr(_native.load(), name)(precision, t.data_ptr(), out.data_ptr(), nx, ny, nz, stream), name)
+    return out
+
+
+def curl_E(E):
+    """Forward-difference curl of E with the reference's edge rule: the
+    difference is dropped on the last plane of its axis (fdtd/grid.py:29-51).
+    Returns a CUDA tensor."""
+    return _curl("fdtd_curl_E", E)
+
+
+def curl_H(H):
+    """Backward-difference curl of H with the reference's edge rule: the
+    difference is dropped on the first plane of its axis (fdtd/grid.py:54-76).
+    Returns a CUDA tensor."""
+    return _curl("fdtd_curl_H", H)
+
 
 class Grid:
     """The FDTD grid: fields, materials and the registered components."""

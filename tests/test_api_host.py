@@ -274,3 +274,10 @@ def test_plotting_helpers_raise(fd):
     for fn in (fd.dB_map_2D, fd.plot_detection, fd.visualization.visualize):
         with pytest.raises(NotImplementedError):
             fn()
+
+
+def test_curl_functions_need_a_gpu(fd):
+    if torch.cuda.is_available():
+        pytest.skip("CUDA present")
+    with pytest.raises(RuntimeError):
+        fd.grid.curl_E(np.zeros((3, 3, 3, 3)))

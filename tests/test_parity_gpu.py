@@ -119,6 +119,16 @@ def _curl_via_abi(native, fn, arr, precision, dtype):
     return out.cpu().numpy()
 
 
+def test_curl_functions_on_reference_known_answers(fd):
+    """fdtd_gb300.grid.curl_E / curl_H, the counterparts of the reference's
+    fdtd.grid.curl_E / curl_H, on the inputs of its known-answer tests."""
+    d = np.load(os.path.join(GOLDEN, "ref_curls.npz"))
+    assert np.array_equal(fd.grid.curl_E(d["E"]).cpu().numpy(), d["curl_E"])
+    assert np.array_equal(fd.grid.curl_H(d["H"]).cpu().numpy(), d["curl_H"])
+    c32 = fd.grid.curl_H(torch.as_tensor(d["H"], dtype=torch.float32)).cpu().numpy()
+    assert c32.dtype == np.float32 and np.allclose(c32, d["curl_H"], rtol=1e-5, atol=1e-5)
+
+
 def test_curls_on_reference_known_answers(native):
     d = np.load(os.path.join(GOLDEN, "ref_curls.npz"))
     assert np.array_equal(_curl_via_abi(native, native.fdtd_curl_E, d["E"], 2, torch.float64), d["curl_E"])
