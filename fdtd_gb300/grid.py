@@ -337,7 +337,7 @@ class Grid:
         plotting (copy grid.E / grid.H to the host and plot them there)."""
         raise NotImplementedError("visualize is not part of the gb300 backend (no plotting)")
 
-    def generate_video(self, *args, **kwargs):
+    def generate_video(self, delete_frames=False):
         """fdtd/grid.py:441-488 calls ffmpeg on plotted frames; not part of this backend."""
         raise NotImplementedError("generate_video is not part of the gb300 backend (no plotting)")
 
