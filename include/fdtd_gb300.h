@@ -174,9 +174,12 @@ typedef struct {
      * table of n value triples (plan element type) and a one-byte index per
      * cell ([nx][ny][nz], nz a multiple of 16) with inv_eps[cell] ==
      * table[index[cell]] for every cell; or n = 1 and index = NULL when every
-     * cell holds table[0].  The staged passes then read one byte per cell, or
-     * nothing, instead of three values.  n = 0: not given.  The caller keeps
-     * the copies consistent with the full arrays. */
+     * cell holds table[0].  The staged passes (and the PML slab kernels of
+     * such plans) then read one byte per cell, or nothing, instead of three
+     * values.  n = 0: not given.  The caller keeps the copies consistent with
+     * the full arrays; an index byte >= n reads zeros.  An index whose
+     * pointer is not 16-byte aligned, or nz not a multiple of 16, leaves the
+     * plan on the full arrays. */
     const void *eps_table;
     int32_t n_eps_table;                /* 0 .. 256 */
     const uint8_t *eps_index;
