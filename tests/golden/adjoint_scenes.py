@@ -176,4 +176,86 @@ class AnisoDftScene:
         return (F.abs() ** 2).sum()
 
 
+class RandomScene:
+    """A random forward scene of tests/test_fuzz_gpu.py (less its
+    PlaneDetector, which the reference lacks) with a design Object or
+    AnisotropicObject on a random box; loss = a random weighting of E^2 and H^2
+    at every line and block detector cell over all steps (the detectors'
+    samples taken from the fields after each step)."""
+
+    steps = 24
+
+    def __init__(self, seed):
+        self.seed = seed
+        self.name = f"adj_random_{seed}"
+
+    def build(self, fd):
+        import os
+        import sys
+
+        here = os.path.dirname(os.path.abspath(__file__))
+        sys.path.insert(0, os.path.dirname(here))
+        from test_fuzz_gpu import random_scene
+
+        grid = random_scene(fd, self.seed, plane_detector=False)
+        bd = getattr(fd, "backend", None)
+        for o in grid.objects:  # the scene sets anisotropic tensors as numpy arrays
+            if bd is not None and isinstance(o.inverse_permittivity, np.ndarray):
+                o.inverse_permittivity = bd.array(o.inverse_permittivity)
+        rng = np.random.default_rng(self.seed + 9000)
+        n = (grid.Nx, grid.Ny, grid.Nz)
+        lo = [int(rng.integers(0, max(1, m - 3))) if m > 1 else 0 for m in n]
+        hi = [min(m, l + int(rng.integers(1, 4))) for l, m in zip(lo, n)]
+        self.box_shape = tuple(h - l for l, h in zip(lo, hi))
+        self.aniso = bool(rng.random() < 0.4)
+        obj = fd.AnisotropicObject(permittivity=2.0, name="design") if self.aniso else fd.Object(
+            permittivity=2.0, name="design")
+        grid[tuple(slice(l, h) for l, h in zip(lo, hi))] = obj
+        for i, d in enumerate(grid.detectors):
+            d.name = f"d{i}"
+        return grid, obj
+
+    def design(self):
+        rng = np.random.default_rng(self.seed + 9100)
+        if self.aniso:
+            t = rng.standard_normal(self.box_shape + (3, 3)) * 0.05
+            return np.eye(3) * rng.uniform(0.3, 0.7, size=self.box_shape + (1, 1)) + (t + np.swapaxes(t, -1, -2))
+        return rng.uniform(0.3, 0.9, size=self.box_shape)
+
+    def weights(self, grid):
+        rng = np.random.default_rng(self.seed + 9200)
+        return {(d.name, f): rng.uniform(0.0, 1.0, size=3) for d in grid.detectors for f in ("E", "H")}
+
+    @staticmethod
+    def _cells(det):
+        if type(det).__name__ == "BlockDetector":
+            return np.ix_(np.asarray(det.x), np.asarray(det.y), np.asarray(det.z))
+        return (np.asarray(det.x), np.asarray(det.y), np.asarray(det.z))
+
+    def ref_loss(self, grid, torch):
+        w = {k: torch.as_tensor(v) for k, v in self.weights(grid).items()}
+        loss = torch.zeros((), dtype=torch.float64)
+        for _ in range(self.steps):
+            grid.step()
+            for d in grid.detectors:
+                cells = tuple(torch.as_tensor(c) for c in self._cells(d))
+                loss = loss + ((grid.E[cells].clone() ** 2) * w[(d.name, "E")]).sum()
+                loss = loss + ((grid.H[cells].clone() ** 2) * w[(d.name, "H")]).sum()
+        return loss
+
+    def detectors(self, fd, grid):
+        # the random scene registers its own; the loss weights follow them
+        self._weights = self.weights(grid)
+
+    def gb_loss(self, outs, torch):
+        total = torch.zeros((), dtype=torch.float64)
+        for (name, field), w in self._weights.items():
+            x = outs[name][field]
+            total = total + ((x.to(torch.float64) ** 2) * torch.as_tensor(w, device=x.device)).sum()
+        return total
+
+
 SCENES = {s.name: s for s in (PlaneScene(), PeriodicScene(True), PeriodicScene(False), AnisoDftScene())}
+
+# random scenes checked on the CPU oracle only (tests/test_adjoint_oracle.py)
+RANDOM_SCENES = {s.name: s for s in (RandomScene(seed) for seed in (0, 1, 3, 4, 6, 8, 10, 11, 12))}

@@ -4,7 +4,8 @@ Usage (needs a checkout of the reference; nothing else in the repository reads i
 
     python tests/golden/make_golden_adjoint.py /root/reference
 
-For every scene of ``adjoint_scenes.SCENES`` the reference package runs with
+For every scene of ``adjoint_scenes.SCENES`` and ``RANDOM_SCENES`` the
+reference package runs with
 its torch.float64 backend and autograd switched back on (the reference turns
 it off at fdtd/backend.py:57-60).  The design object's inverse permittivity is
 replaced by a tensor that requires grad (expanded over the three components
@@ -23,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 
 
-def main(ref_path):
+def main(ref_path, only=None):
     sys.path.insert(0, HERE)
     sys.path.insert(0, REPO)
     from make_golden import load_reference
@@ -35,7 +36,9 @@ def main(ref_path):
 
     fdtd.set_backend("torch.float64")
     torch.set_grad_enabled(True)
-    for name, sc in adjoint_scenes.SCENES.items():
+    for name, sc in list(adjoint_scenes.SCENES.items()) + list(adjoint_scenes.RANDOM_SCENES.items()):
+        if only and name not in only:
+            continue
         grid, obj = sc.build(fdtd)
         p = torch.tensor(sc.design(), dtype=torch.float64, requires_grad=True)
         if p.ndim == 5:
@@ -50,4 +53,5 @@ def main(ref_path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # optional further arguments: only these scenes
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:] or None)

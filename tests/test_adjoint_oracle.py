@@ -36,10 +36,10 @@ def oracle_loss_and_grad(sc, design_values):
     return float(loss.detach()), grad
 
 
-@pytest.mark.parametrize("name", sorted(adjoint_scenes.SCENES))
+@pytest.mark.parametrize("name", sorted(adjoint_scenes.SCENES) + sorted(adjoint_scenes.RANDOM_SCENES))
 def test_adjoint_oracle_matches_reference_autograd(name):
     ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
-    sc = adjoint_scenes.SCENES[name]
+    sc = adjoint_scenes.SCENES.get(name) or adjoint_scenes.RANDOM_SCENES[name]
     loss, grad = oracle_loss_and_grad(sc, ref["design"])
     assert abs(loss - float(ref["loss"])) <= 1e-12 * abs(float(ref["loss"]))
     err = np.linalg.norm(grad - ref["grad"]) / np.linalg.norm(ref["grad"])
