@@ -193,8 +193,9 @@ class RandomScene:
         import os
         import sys
 
-        here = os.path.dirname(os.path.abspath(__file__))
-        sys.path.insert(0, os.path.dirname(here))
+        tests_dir = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        if tests_dir not in sys.path:
+            sys.path.insert(0, tests_dir)
         from test_fuzz_gpu import random_scene
 
         grid = random_scene(fd, self.seed, plane_detector=False)
