@@ -10,17 +10,23 @@ than L2, so no flush is needed between steps.
 
 Printed line (rank 0): value = float32 Gcell-updates/s of all ranks, with
 the float64 and compensated float32 runs of the same grid, the float32 /
-float64 detector-trace error, the roofline of the fused half-step kernels
-(HBM-bound), the CPU oracle on a crop of the same generator, the end-to-end
-figure through the public API with per-step host<->device copies, launch
-count and SM clocks sampled during the timed region, and the cost of a
-differentiable run (adjoint) over a forward run on configs 4 and 5, with the
-config-4 gradient checked against central finite differences.
+float64 detector-trace error (the timed records and the 1000-step run), the
+roofline of the fused half-step kernels (HBM-bound), the end-to-end figure
+through the public API with per-step host<->device copies, launch count and
+SM clocks sampled during the timed region; configs 2 and 5 at full size
+(throughput and HBM fraction per precision, long-run float32 / float32c
+error against float64: config 2's block detector over 2000 steps, config
+5's DFT accumulators); the cost of a differentiable run (adjoint) over a
+forward run on configs 4 and 5, with the config-4 gradient checked against
+central finite differences; and the reference's own CPU time step (its
+numpy backend, and its torch.float64 backend on all host threads) on a
+128^3 crop of the config-3 generator.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-``--impl reference`` times the reference algorithm's CPU implementation (the
-numpy oracle port of fdtd's time step) on a crop of the same workload.
+``--impl reference`` times the reference's own numpy time step (the
+unmodified package installed in baseline/_ref; the oracle port of it only if
+that is absent) on the same 128^3 crop, one contract step per time step.
 N > 1 runs one independent replica per rank (the path has no exchange step).
 """
 
@@ -63,7 +69,7 @@ def parse():
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference", "reference-gpu"], default="gb300",
-                   help="reference: the reference's numpy time step on the host cores (restated); "
+                   help="reference: the reference's own numpy time step on the host cores; "
                         "reference-gpu: the reference's own torch CUDA backend from baseline/_ref")
     p.add_argument("--ref-backend", default="torch.cuda.float64",
                    help="backend name of the reference for --impl reference-gpu")
@@ -84,6 +90,12 @@ def parse():
     p.add_argument("--adjoint-only", choices=["c4", "c5", "both"], default=None,
                    help="only the adjoint/forward timing of the named configs (prints its own JSON line)")
     p.add_argument("--only", choices=["float32", "float32c", "float64"], default=None)
+    p.add_argument("--error-steps", type=int, default=1000,
+                   help="config 3: steps of the long-run float32 / float32c trace error against float64 (0 = off)")
+    p.add_argument("--skip-configs", action="store_true",
+                   help="skip configs 2 and 5 (forward throughput, roofline and long-run errors)")
+    p.add_argument("--configs-only", action="store_true",
+                   help="only configs 2 and 5 (prints its own JSON line)")
     return p.parse_args()
 
 
@@ -304,32 +316,89 @@ def run_precision(prec, args, dist, fd, scenes, eps, want_halves, want_e2e, samp
                       "d2h_bytes_per_step": int(host[0].numel() * host.element_size()),
                       "how": "per step: grid.step() (host waveform -> pinned -> device, fused kernels via the "
                              "C ABI) then the step's detector record copied device -> pinned host"}
+    if args.error_steps and g.time_steps_passed < args.error_steps:
+        # same physical steps in every precision (runs, half steps, single
+        # steps): continue to the long-run length and keep that trace
+        g.run(args.error_steps - g.time_steps_passed, progress_bar=False)
+        torch.cuda.synchronize()
+        out["trace_long"] = g.detector.E.tensor()[: args.error_steps].double().cpu()
     del g, eng
     gc.collect()  # grids and their components reference each other
     torch.cuda.empty_cache()
     return out
 
 
-def cpu_oracle_rate(budget_s, n_full):
-    """Time the numpy oracle (one core) on a crop of the config-3 generator."""
-    from fdtd_gb300 import scenes
-    from oracle import fdtd_oracle as fo
+CPU_CROP = 128  # edge of the config-3 crop every CPU figure runs on
 
-    n = 96
-    g = scenes.c3(fo, n=n, pml=3, detector=True)
-    g.step()
-    t0 = time.perf_counter()
-    g.step()
-    per = time.perf_counter() - t0
-    steps = int(max(3, min(2000, budget_s / max(per, 1e-3))))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        g.step()
-    dt = time.perf_counter() - t0
-    return {"value": n ** 3 * steps / dt / 1e9, "unit": UNIT, "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
-            "sample": f"numpy float64 oracle of fdtd's time step on the config-3 generator cropped to {n}^3 "
-                      f"(3-cell PML, periodic x, point source, line detector), {steps} steps, "
-                      f"{dt:.1f} s, one host core (numpy elementwise is single-threaded)"}
+
+def reference_module():
+    """The unmodified reference package installed in baseline/_ref (pip
+    install of the reference), imported with the no-op matplotlib stand-in
+    its plotting module needs (and a tqdm stand-in where tqdm is absent);
+    None when it is not installed."""
+    ref_dir = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isfile(os.path.join(ref_dir, "fdtd", "__init__.py")):
+        return None
+    for p in (ref_dir, os.path.join(ROOT, "tests", "golden", "mplstub")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    stub = os.path.join(ROOT, "tests", "golden", "tqdmstub")
+    if stub not in sys.path:
+        sys.path.append(stub)
+    import fdtd as ref
+
+    return ref
+
+
+def cpu_rate(backend="numpy", steps=None, budget_s=None, warmup=1, n=CPU_CROP):
+    """Gcell-updates/s of the reference's own CPU time step (``backend``
+    "numpy" or "torch.float64") on the config-3 generator cropped to n^3,
+    either for ``steps`` timed steps or for about ``budget_s`` seconds.
+    Falls back to the oracle port of the numpy time step when the reference
+    is not installed."""
+    import torch
+
+    from fdtd_gb300 import scenes
+
+    pml = max(2, int(round(20 * n / 768)))
+    dtype0 = torch.get_default_dtype()  # importing the reference sets float64
+    ref = reference_module()
+    threads = 1
+    if ref is not None:
+        ref.set_backend(backend)
+        mod, kind = ref, "reference"
+        if backend.startswith("torch"):
+            threads = torch.get_num_threads()
+    else:
+        if backend != "numpy":
+            return None
+        from oracle import fdtd_oracle as fo
+
+        mod, kind = fo, "port"
+    try:
+        g = scenes.c3(mod, n=n, pml=pml, detector=True)
+        run = (lambda k: g.run(k, progress_bar=False)) if kind == "reference" else g.run
+        run(max(1, warmup))
+        if steps is None:
+            t0 = time.perf_counter()
+            run(1)
+            per = time.perf_counter() - t0
+            steps = int(max(3, min(2000, budget_s / max(per, 1e-4))))
+        t0 = time.perf_counter()
+        run(steps)
+        dt = time.perf_counter() - t0
+    finally:
+        if ref is not None:
+            ref.set_backend("numpy")
+        torch.set_default_dtype(dtype0)
+    what = {"reference": f"the reference's own {backend} backend (baseline/_ref, unmodified)",
+            "port": "the numpy oracle port of the reference's time step (reference not installed)"}[kind]
+    return {"value": n ** 3 * steps / dt / 1e9, "unit": UNIT, "cores": threads, "host_cores": os.cpu_count(),
+            "kind": kind, "steps": steps, "seconds": dt,
+            "sample": f"{what}, float64, on the config-3 generator cropped to {n}^3 ({pml}-cell PML on y/z, "
+                      f"periodic x, centre point source, x line detector), {steps} steps in {dt:.1f} s, "
+                      + ("one host core (numpy elementwise is single-threaded)" if threads == 1 else
+                         f"{threads} torch threads")}
 
 
 def c4_finite_differences(fd, scenes, grad, loss_of, voxels=16, h=1e-3, seed=4):
@@ -429,6 +498,78 @@ def adjoint_ratio(fd, scenes, which, fd_check=True):
     return out
 
 
+def config_runs(fd, scenes, which=("c2", "c5")):
+    """Configs 2 and 5 at full size in float64, float32 and float32c from zero
+    fields: forward Gcell-updates/s and the fraction of the measured HBM
+    bandwidth by the algorithmic bytes of the step (CUDA events around the
+    whole run), and the long-run error of float32 / float32c against float64
+    on the same grid: config 2 the 33^3 BlockDetector E and H records over
+    2000 steps, config 5 the float64 DFT accumulators after 2000 steps."""
+    import torch
+
+    peak, _ = peaks()
+    out = {}
+    for cfg in which:
+        if cfg == "c2":
+            steps = 2000
+            eps = scenes.c2_permittivity(256)
+            make = lambda: scenes.c2(fd, eps=eps)
+            desc = ("256^3 uniaxial random eps ~ U[1,12] smoothed by a 3-cell box filter, 16-cell PML, "
+                    "AbsorbingObject 64^3 sigma 1e4 S/m, x-polarised PlaneSource z=20, 33^3 BlockDetector")
+        else:
+            steps = 2000
+            make = lambda: scenes.c5(fd)
+            desc = ("384x384x192, 20-cell PML, 96x96x48 AnisotropicObject (random SPD), Gaussian PlaneSource "
+                    "z=24, float64 DFT plane z=168 at 1500/1550/1600 nm")
+        res, ref_out = {}, None
+        for prec in ("float64", "float32", "float32c"):
+            fd.set_backend("gb300." + prec)
+            g = make()
+            g.run(3, progress_bar=False)  # plan, material copies and kernels loaded
+            del g
+            gc.collect()
+            g = make()
+            eng = g._ensure_engine()
+            eng.refresh()
+            cells = g.Nx * g.Ny * g.Nz
+            layout = eng.compact_materials()
+            slabs = slab_cells(g) * SLAB_BYTES[prec]
+            step_bytes = cells * (half_bytes(prec, layout[0]) + half_bytes(prec, layout[1])) + 2 * slabs
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            g.run(steps, progress_bar=False)
+            e1.record()
+            torch.cuda.synchronize()
+            eng.check_status()
+            ms = e0.elapsed_time(e1)
+            det = g.detectors[0]
+            if cfg == "c2":
+                rec = (det.E.tensor().double(), det.H.tensor().double())
+            else:
+                rec = (det.dft.clone(),)
+            res[prec] = {"value": cells * steps / (ms * 1e-3) / 1e9, "ms_per_step": ms / steps,
+                         "hbm_frac": step_bytes * steps / (ms * 1e-3) / 1e9 / peak,
+                         "algo_bytes_per_step": step_bytes, "tiling": eng.tiling(),
+                         "materials": {"E": layout[0], "H": layout[1]}}
+            if prec == "float64":
+                ref_out = rec
+            else:
+                res[prec]["rel_l2_vs_fp64"] = [float((a - b).abs().norm() / b.abs().norm())
+                                               for a, b in zip(rec, ref_out)]
+            del g, eng, det, rec
+            gc.collect()
+            torch.cuda.empty_cache()
+        out[cfg] = {"workload": desc, "steps": steps, "runs": res,
+                    "error_of": "BlockDetector E and H records" if cfg == "c2" else "DFT accumulators",
+                    "hbm_peak_gbs": peak}
+        del ref_out
+        gc.collect()
+        torch.cuda.empty_cache()
+    fd.set_backend("gb300.float32")
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -512,13 +653,29 @@ def gb300_arm(args):
                 errs[prec] = float((tr - ref).norm() / ref.norm())
         line["error"] = {"trace_rel_l2_vs_fp64": errs, "records": int(ref.shape[0]),
                          "detector": "line along x through the source"}
+        if "trace_long" in f64:
+            refl = f64["trace_long"]
+            line["error"]["c3"] = {
+                "records": int(refl.shape[0]), "detector": "line along x through the source",
+                "trace_rel_l2_vs_fp64": {p: float((res[p]["trace_long"] - refl).norm() / refl.norm())
+                                         for p in ("float32", "float32c") if "trace_long" in res[p]}}
     if "float32c" in res:
         line["fp32c"] = {"value": res["float32c"]["gcells"], "ms_per_step": res["float32c"]["ms_per_step"]}
     line["nonfinite"] = {p: r["stats"]["nonfinite"] for p, r in res.items()}
+    if dist.rank == 0 and not args.skip_configs and args.n == 768:
+        line["configs"] = config_runs(fd, scenes)
+        if "error" in line:
+            for cfg, r in line["configs"].items():
+                line["error"][cfg] = {"steps": r["steps"], "of": r["error_of"],
+                                      "rel_l2_vs_fp64": {p: r["runs"][p]["rel_l2_vs_fp64"]
+                                                         for p in ("float32", "float32c")}}
     if dist.rank == 0 and not args.skip_adjoint:
         line["adjoint"] = adjoint_ratio(fd, scenes, ["c4", "c5"])
     if dist.rank == 0 and not args.skip_cpu:
-        line["cpu_baseline"] = cpu_oracle_rate(args.cpu_seconds, n)
+        line["cpu_baseline"] = cpu_rate("numpy", budget_s=args.cpu_seconds)
+        torch_cpu = cpu_rate("torch.float64", budget_s=args.cpu_seconds / 2)
+        if torch_cpu is not None:
+            line["cpu_baseline_torch"] = torch_cpu
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
@@ -528,50 +685,33 @@ def gb300_arm(args):
 # reference arm: the CPU implementation of the algorithm (numpy oracle port)
 # --------------------------------------------------------------------------
 def reference_arm(args):
+    """The reference's own CPU time step: its numpy backend (the unmodified
+    package in baseline/_ref) on the host, one step per step of the contract,
+    on the config-3 crop every CPU figure uses.  numpy elementwise runs on one
+    core; the reference's torch.float64 CPU backend (all threads) is the
+    second CPU figure of the GPU arm's line."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from fdtd_gb300 import scenes
-    from oracle import fdtd_oracle as fo
-
-    # crop of the config-3 generator sized so that warmup + steps fit about two minutes
-    g = scenes.c3(fo, n=48, pml=2, detector=True)
-    t0 = time.perf_counter()
-    g.step()
-    rate = 48 ** 3 / max(time.perf_counter() - t0, 1e-4)
-    budget = 120.0
-    n = int((rate * budget / max(1, args.steps + args.warmup)) ** (1.0 / 3.0))
-    n = max(24, min(args.n, 160, n))
-    pml = max(2, int(round(20 * n / 768)))
-    g = scenes.c3(fo, n=n, pml=pml, detector=True)
-    for _ in range(args.warmup):
-        g.step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        g.step()
-    dt = time.perf_counter() - t0
-    value = n ** 3 * args.steps / dt / 1e9
-    sample = (f"numpy float64 oracle (port of fdtd's numpy time step) on the config-3 generator cropped to "
-              f"{n}^3 ({pml}-cell PML, periodic x, point source, line detector); one host core")
+    r = cpu_rate("numpy", steps=args.steps, warmup=args.warmup)
     line = {
         "impl": "reference",
         "metric": METRIC,
-        "value": value,
+        "value": r["value"],
         "unit": UNIT,
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": dt / args.steps * 1e3,
+        "ms_per_step": r["seconds"] / args.steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: config-3 generator (seed 3), zero initial fields",
-        "config": {"workload": f"config3_{args.n}^3_float32", "sample_grid": [n, n, n],
+        "config": {"workload": f"config3_{args.n}^3_float32", "sample_grid": [CPU_CROP] * 3,
                    "parallelism": "single host process"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
-                         "sample": sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": r,
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -586,15 +726,12 @@ def reference_gpu_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    ref_dir = os.path.join(ROOT, "baseline", "_ref")
-    if not os.path.isfile(os.path.join(ref_dir, "fdtd", "__init__.py")):
+    ref = reference_module()
+    if ref is None:
         print(json.dumps({"impl": "reference-gpu", "unavailable": "reference not installed in baseline/_ref"}))
         return
-    sys.path[:0] = [ref_dir, os.path.join(ROOT, "tests", "golden", "mplstub")]
-    sys.path.append(os.path.join(ROOT, "tests", "golden", "tqdmstub"))  # only if tqdm is absent
     import torch
 
-    import fdtd as ref
     from fdtd_gb300 import scenes
 
     ref.set_backend(args.ref_backend)
@@ -630,6 +767,11 @@ def main():
         reference_arm(args)
     elif args.impl == "reference-gpu":
         reference_gpu_arm(args)
+    elif args.configs_only:
+        import fdtd_gb300 as fd
+        from fdtd_gb300 import scenes
+
+        print(json.dumps({"configs": config_runs(fd, scenes)}), flush=True)
     elif args.adjoint_only:
         import fdtd_gb300 as fd
         from fdtd_gb300 import scenes

@@ -12,6 +12,11 @@ kernel pass through the C ABI in include/fdtd_gb300.h.
     ...
     grid.run(500)
 
+The reference package itself selects this backend once
+``fdtd_gb300.install(fdtd)`` has wrapped its ``set_backend``:
+``fdtd.set_backend("gb300.float32")`` then routes ``fdtd.Grid`` and the
+component classes here (``fdtd_gb300.plugin``).
+
 Gradients with respect to design objects' inverse permittivity come from a
 reverse-time adjoint behind torch.autograd (``fdtd_gb300.adjoint.run``).
 """
@@ -26,6 +31,7 @@ from .grid import Grid
 from .objects import AbsorbingObject, AnisotropicObject, Object
 from .sources import GaussianPlaneSource, LineSource, PlaneSource, PointSource, SoftArbitraryPointSource
 from . import adjoint, constants, waveforms, conversions, visualization
+from .plugin import install, uninstall
 from .visualization import dB_map_2D, plot_detection
 
 __all__ = [
@@ -33,5 +39,5 @@ __all__ = [
     "AnisotropicObject", "PointSource", "LineSource", "PlaneSource", "GaussianPlaneSource",
     "SoftArbitraryPointSource", "LineDetector", "BlockDetector", "CurrentDetector", "PlaneDetector",
     "DFTPlaneDetector", "FrequencyRoutines", "backend", "set_backend", "adjoint", "constants", "waveforms",
-    "conversions", "visualization", "dB_map_2D", "plot_detection",
+    "conversions", "visualization", "dB_map_2D", "plot_detection", "install", "uninstall",
 ]

@@ -700,7 +700,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.kf.nslab_fused = p.fused_slabs;
     }
 
-    p.stats_ctas = 152 * 4;
+    p.stats_ctas = std::max(1, std::min(4 * n_sm, FDTD_STATS_STATIC_MAX_ROWS));
+    p.device = dev;
     p.launches_per_step = 2 + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
                           (p.n_current > 0 ? 1 : 0) + (int)p.dft.size();
     return FDTD_OK;
@@ -900,19 +901,51 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_rows_mutex;
 double *g_rows_addr[kMaxDevices] = {nullptr};
+CUcontext g_rows_ctx[kMaxDevices] = {nullptr};
 
-// Device address of g_stats_rows on the current device (looked up on first use).
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+
+// The driver's cuCtxGetCurrent, found through the runtime (the library links
+// no driver import library).
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = nullptr;
+    if (fn == nullptr) {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrentFn>(ptr);
+    }
+    return fn;
+}
+
+// Device address of g_stats_rows on the current device, looked up once per
+// device with that device current and kept.  The context it was looked up
+// in is kept too: after a device reset (cudaDeviceReset, or a new primary
+// context) the old address is stale, and the first call in the new context
+// looks it up again.
 int stats_rows_address(double **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e);
     if (dev < 0 || dev >= kMaxDevices) return FDTD_ERR_UNSUPPORTED;
+    CtxGetCurrentFn get = ctx_get_current();
+    auto current = [&]() {
+        CUcontext c = nullptr;
+        if (get == nullptr || get(&c) != CUDA_SUCCESS) c = nullptr;
+        return c;
+    };
+    // a thread that has not used the runtime yet has no current context: the
+    // lookup below binds the device's primary context to it
+    CUcontext ctx = current();
     std::lock_guard<std::mutex> lock(g_rows_mutex);
-    if (g_rows_addr[dev] == nullptr) {
+    if (g_rows_addr[dev] == nullptr || ctx == nullptr || g_rows_ctx[dev] != ctx) {
         void *ptr = nullptr;
         e = cudaGetSymbolAddress(&ptr, g_stats_rows);
         if (e != cudaSuccess) return cuda_fail(e);
         g_rows_addr[dev] = static_cast<double *>(ptr);
+        g_rows_ctx[dev] = current();
     }
     *out = g_rows_addr[dev];
     return FDTD_OK;
@@ -926,6 +959,11 @@ int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_row
     const Plan &p = plan->p;
     const int rows = n_rows ? n_rows : p.stats_ctas;
     if (rows > FDTD_STATS_STATIC_MAX_ROWS) return FDTD_ERR_RANGE;
+    // the array used is the current device's: it must be the plan's device
+    int cur = 0;
+    cudaError_t ce = cudaGetDevice(&cur);
+    if (ce != cudaSuccess) return cuda_fail(ce);
+    if (cur != p.device) return FDTD_ERR_ARGUMENT;
     double *part = nullptr;
     const int rc = stats_rows_address(&part);
     if (rc != FDTD_OK) return rc;

@@ -48,7 +48,8 @@ struct Plan {
     std::vector<fdtd_dft_desc> dft;
     int n_columns, n_phase_columns;
     void *dev_mem;     // the plan's own device tables
-    int stats_ctas;
+    int stats_ctas;    // partial rows of the field statistics: 4 per SM, at most FDTD_STATS_STATIC_MAX_ROWS
+    int device;        // CUDA device the plan was created on
     int launches_per_step;
     // reverse-time adjoint: launch shape of k_adj_E / k_adj_H, host copies of
     // the items (objects, then E sources, then H sources), the grid.boundaries

@@ -23,7 +23,8 @@
 // tiles reach past the grid edges where the differences are dropped; the
 // TMA unit fills out-of-range rows and columns with zeros.  Every mbarrier
 // wait is bounded: on expiry the CTA records bit 0 in the plan's status word,
-// drains its outstanding copies (bounded again) and returns.
+// drains its outstanding copies (bounded again; bit 1 when a drain wait also
+// expires) and returns.
 #pragma once
 
 #include <cuda.h>
@@ -344,7 +345,10 @@ __global__ void __launch_bounds__(TZ *TY)
     }
     if (abort_flag && tid == 0) {
         atomicOr(g.status, 1);
-        for (int q = r; q < issued; ++q) mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1));
+        // a drain wait that also runs out leaves copies into shared memory in
+        // flight after the CTA exits: bit 1 marks later results untrusted
+        for (int q = r; q < issued; ++q)
+            if (!mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1))) atomicOr(g.status, 2);
     }
 }
 
@@ -452,7 +456,10 @@ __global__ void __launch_bounds__(TZ *TY)
     }
     if (abort_flag && tid == 0) {
         atomicOr(g.status, 1);
-        for (int q = r; q < issued; ++q) mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1));
+        // a drain wait that also runs out leaves copies into shared memory in
+        // flight after the CTA exits: bit 1 marks later results untrusted
+        for (int q = r; q < issued; ++q)
+            if (!mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1))) atomicOr(g.status, 2);
     }
 }
 

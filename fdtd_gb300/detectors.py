@@ -239,6 +239,10 @@ class DFTPlaneDetector(_Detector):
         """Clear the accumulated transform."""
         self.dft.zero_()
 
+    def detector_values(self):
+        """Outputs of the detector, {'dft': (frequencies, *box, 3) complex128}."""
+        return {"dft": self.dft}
+
 
 class CurrentDetector(_Detector):
     """Current around a point after every H half step (fdtd/detectors.py:284-496).

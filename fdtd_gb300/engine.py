@@ -160,8 +160,10 @@ class _PinnedStager:
         host.numpy()[:] = array.reshape(-1)
         dev = torch.empty(n, dtype=torch.float64, device=device)
         dev.copy_(host, non_blocking=True)
+        # the copy runs on the current stream of the tensor's device; the event
+        # that guards the pinned buffer's reuse must follow that stream
         ev = torch.cuda.Event()
-        ev.record()
+        ev.record(torch.cuda.current_stream(dev.device))
         self._events[k] = ev
         return dev
 
@@ -534,13 +536,13 @@ class Engine:
         (cos, -sin) of 2 pi f q dt for the step indices q in ``steps``."""
         g = self.grid
         ph = np.empty((len(steps), self.n_phase, 2), dtype=np.float64)
+        t = np.asarray(steps, dtype=np.float64) * g.time_step
         col = 0
         for det in self.dfts:
             for f in det.frequencies:
-                for r, q in enumerate(steps):
-                    theta = 2.0 * math.pi * f * (q * g.time_step)
-                    ph[r, col, 0] = math.cos(theta)
-                    ph[r, col, 1] = -math.sin(theta)
+                theta = (2.0 * math.pi * f) * t
+                ph[:, col, 0] = np.cos(theta)
+                ph[:, col, 1] = -np.sin(theta)
                 col += 1
         return ph
 
@@ -553,8 +555,8 @@ class Engine:
         if self.sources:
             tab = np.empty((n, len(self.sources)), dtype=np.float64)
             for c, s in enumerate(self.sources):
-                for r in range(n):
-                    tab[r, c] = s._value(q0 + r)
+                # the reference's scalar expressions (math.sin), one per step
+                tab[:, c] = [s._value(q) for q in range(q0, q0 + n)]
             wave = self._wave_stage.upload(tab, g._device)
         if self.n_phase and dft:
             phase = self.upload_phase(self.phase_table(range(q0, q0 + n)))
@@ -588,9 +590,7 @@ class Engine:
                     if hasattr(src, "current_detector") and src.current_detector in self.cur_ranges:
                         det = src.current_detector
                         frozen = sum(c.shape[0] for c in det._frozen["I"])
-                        for k in range(n):
-                            r = self.rec_I + k - 1
-                            src._steps.append((q0 + k, frozen + r if (q0 + k > 0 and r >= 0) else -1))
+                        src._note_steps(q0, n, frozen, self.rec_I - 1)
         stream = ctypes.c_void_p(torch.cuda.current_stream(g._device).cuda_stream)
         if capture is None:
             _native.check(lib.fdtd_run(self.plan, ctypes.byref(a), stream), "fdtd_run")

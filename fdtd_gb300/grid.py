@@ -359,15 +359,21 @@ class Grid:
         return self.folder
 
     def save_data(self):
-        """Write every detector's E and H records to ``detector_readings.npz``
-        (keys '<name> (E)' and '<name> (H)'), read straight from the device traces."""
+        """Write the detector records to ``detector_readings.npz`` in the folder
+        of ``save_simulation`` (fdtd/grid.py:490-514), read straight from the
+        device traces: for every detector the keys '<name> (E)' and
+        '<name> (H)', each an array of shape (steps, *record).  Detectors
+        without E/H records (the reference raises KeyError there) store their
+        own outputs instead: a CurrentDetector '<name> (I)', a DFTPlaneDetector
+        '<name> (dft)'."""
         if self.folder is None:
             raise Exception("Save location not initialized. Please read about "
                             "'fdtd.Grid.saveSimulation()' or try running 'grid.saveSimulation()'.")
         dic = {}
         for det in self.detectors:
             vals = det.detector_values()
-            for key in ("E", "H"):
-                if key in vals:
-                    dic[f"{det.name} ({key})"] = np.asarray(vals[key])
+            keys = ("E", "H") if ("E" in vals or "H" in vals) else tuple(vals)
+            for key in keys:
+                v = vals[key]
+                dic[f"{det.name} ({key})"] = v.detach().cpu().numpy() if hasattr(v, "detach") else np.asarray(v)
         np.savez(os.path.join(self.folder, "detector_readings"), **dic)

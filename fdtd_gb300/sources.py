@@ -294,7 +294,10 @@ class SoftArbitraryPointSource:
         self.current_detector = None
         self.waveform_array = waveform_array
         self.impedance = impedance
-        self._steps = []  # per E half: (step index, index of the current record it used or -1)
+        # E halves run so far, as runs [q0, n, frozen, r0]: step q0 + k used the
+        # current record frozen + r0 + k (none at step 0 or for r0 + k < 0);
+        # contiguous calls extend the last run, so stepping adds no entries
+        self._runs = []
 
     def _register_grid(self, grid, x, y, z):
         from .detectors import CurrentDetector
@@ -323,10 +326,26 @@ class SoftArbitraryPointSource:
         return [("E", "feedback", 2, (self.x, self.y, self.z), (self.x + 1, self.y + 1, self.z + 1),
                  float(self.impedance))]
 
+    def _note_steps(self, q0, n, frozen, r0):
+        """Record n E halves from step q0 whose first used current record r0."""
+        if self._runs:
+            last = self._runs[-1]
+            if q0 == last[0] + last[1] and frozen == last[2] and r0 == last[3] + last[1]:
+                last[1] += n
+                return
+        self._runs.append([q0, n, frozen, r0])
+
+    def _steps(self):
+        """(step index, index of the current record it used or -1) per E half."""
+        for q0, n, frozen, r0 in self._runs:
+            for k in range(n):
+                r = r0 + k
+                yield q0 + k, (frozen + r if (q0 + k > 0 and r >= 0) else -1)
+
     def _voltages(self):
         ins, outs = [], []
         I = self.current_detector.I
-        for q, r in self._steps:
+        for q, r in self._steps():
             vin = self._value(q)
             cur = float(I[r].reshape(-1)[0]) if r >= 0 else 0.0
             vout = vin + self.impedance * cur if self.impedance > 0 else vin

@@ -219,7 +219,9 @@ int fdtd_plan_destroy(fdtd_plan *plan);
 
 /* Device status word of the plan, copied to *out after synchronising the
  * stream: 0 = healthy; bit 0 = a staged kernel's pipeline wait expired (the
- * step's results are invalid).  reset != 0 clears the word afterwards.  No
+ * step's results are invalid); bit 1 = besides, a CTA gave up waiting for its
+ * own copies in flight (results of later kernels on this context are
+ * untrusted too).  reset != 0 clears the word afterwards.  No
  * reference counterpart (the reference cannot fail this way). */
 int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t stream);
 
@@ -320,9 +322,13 @@ int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_s
  * n_rows = number of partial rows (CTAs) to use, 0 = the plan's default (the
  * same rows fdtd_field_stats uses, so both give identical results); a value
  * above FDTD_STATS_STATIC_MAX_ROWS returns FDTD_ERR_RANGE without launching.
+ * The current device must be the plan's device (else FDTD_ERR_ARGUMENT).
  * The first call on a device looks up the array's device address (with that
- * device current) and keeps it; make that first call before any stream
- * capture.  All calls share the array and it keeps the last call's contents
+ * device current) and keeps it with the context it belongs to; make that
+ * first call before any stream capture.  After a device reset
+ * (cudaDeviceReset, a new primary context) the kept address is stale: the
+ * first call in the new context looks it up again, so make that call before
+ * any capture too.  All calls share the array and it keeps the last call's contents
  * (every row used is rewritten before it is read, so nothing needs clearing);
  * calls that overlap on the GPU race with each other.  No counterpart in the
  * reference (the reference has no health check). */

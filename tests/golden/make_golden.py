@@ -2,7 +2,7 @@
 
 Usage (needs a checkout of the reference; nothing else in the repository reads it):
 
-    python tests/golden/make_golden.py /root/reference [scene ...]
+    python tests/golden/make_golden.py <path to the reference checkout> [scene ...]
 
 The reference imports matplotlib for plotting only; a no-op stand-in from
 ``tests/golden/mplstub`` is put on ``sys.path`` first.  Outputs:
@@ -14,6 +14,9 @@ The reference imports matplotlib for plotting only; a no-op stand-in from
   ``golden_scenes.SCENES`` after its stated number of steps.
 * ``ref_fuzz.npz`` -- the same for the first random forward scenes of
   ``tests/test_fuzz_gpu.py`` (scene argument ``fuzz``).
+* ``ref_c1_full.npz`` -- config 1 at its full size and step count (scene
+  argument ``c1_full``, only when named): traces, three planes of the final
+  fields and digests of the whole final fields.
 """
 
 import os
@@ -72,6 +75,29 @@ def fuzz_fixture(fdtd):
     return out
 
 
+FULL_C1_PLANES = (5, 32, 58)  # x planes kept of the full fields: low PML, centre, high PML
+
+
+def full_c1_fixture(fdtd):
+    """Config 1 at its full size (64^3, 10-cell PML on six faces, Object
+    2.25 at 24:40, point source, x line detector, 500 steps): the detector
+    traces, three x planes of the final E and H, and SHA-256 digests and sums
+    of squares of the whole final fields (full fields would be 12 MB)."""
+    import hashlib
+
+    from fdtd_gb300 import scenes
+
+    grid = scenes.c1(fdtd)
+    grid.run(500, progress_bar=False)
+    E, H = np.ascontiguousarray(grid.E, np.float64), np.ascontiguousarray(grid.H, np.float64)
+    det = grid.detectors[0]
+    return dict(steps=np.array(500), trace_E=np.array(det.E), trace_H=np.array(det.H),
+                planes=np.array(FULL_C1_PLANES), E_planes=E[list(FULL_C1_PLANES)],
+                H_planes=H[list(FULL_C1_PLANES)], E_sha256=np.array(hashlib.sha256(E.tobytes()).hexdigest()),
+                H_sha256=np.array(hashlib.sha256(H.tobytes()).hexdigest()),
+                E_sumsq=np.array(float((E * E).sum())), H_sumsq=np.array(float((H * H).sum())))
+
+
 def main(ref_path, only=None):
     fdtd = load_reference(ref_path)
     sys.path.insert(0, REPO)
@@ -83,6 +109,9 @@ def main(ref_path, only=None):
     H1 = np.random.RandomState(1).randn(3, 3, 3, 3)
     np.savez(os.path.join(HERE, "ref_curls.npz"), E=E0, curl_E=curl_E(E0), H=H1, curl_H=curl_H(H1),
              reference_version=fdtd.__version__)
+    if only and "c1_full" in only:
+        np.savez_compressed(os.path.join(HERE, "ref_c1_full.npz"), **full_c1_fixture(fdtd))
+        print("c1_full")
     if not only or "fuzz" in only:
         np.savez_compressed(os.path.join(HERE, "ref_fuzz.npz"), **fuzz_fixture(fdtd))
         print("fuzz", len(FUZZ_SEEDS), "seeds")
@@ -101,4 +130,6 @@ def main(ref_path, only=None):
 
 if __name__ == "__main__":
     # optional further arguments: only these scenes
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:] or None)
+    if len(sys.argv) < 2:
+        sys.exit(__doc__)
+    main(sys.argv[1], sys.argv[2:] or None)

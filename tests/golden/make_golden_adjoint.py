@@ -2,7 +2,7 @@
 
 Usage (needs a checkout of the reference; nothing else in the repository reads it):
 
-    python tests/golden/make_golden_adjoint.py /root/reference
+    python tests/golden/make_golden_adjoint.py <path to the reference checkout>
 
 For every scene of ``adjoint_scenes.SCENES`` and ``RANDOM_SCENES`` the
 reference package runs with
@@ -54,4 +54,6 @@ def main(ref_path, only=None):
 
 if __name__ == "__main__":
     # optional further arguments: only these scenes
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:] or None)
+    if len(sys.argv) < 2:
+        sys.exit(__doc__)
+    main(sys.argv[1], sys.argv[2:] or None)

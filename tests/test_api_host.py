@@ -6,6 +6,8 @@ tests/test_backend.py:22-26) plus the registration rules the fused kernels
 rely on.  Nothing here runs a time step.
 """
 
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -281,3 +283,22 @@ def test_curl_functions_need_a_gpu(fd):
         pytest.skip("CUDA present")
     with pytest.raises(RuntimeError):
         fd.grid.curl_E(np.zeros((3, 3, 3, 3)))
+
+
+def test_save_data_keys_without_steps(fd, tmp_path, monkeypatch):
+    """Grid.save_data before any step: both '(E)' and '(H)' keys for every
+    E/H detector (fdtd/grid.py:508-513), empty record arrays; a DFT plane
+    detector stores its accumulators."""
+    monkeypatch.chdir(tmp_path)
+    g = fd.Grid((10, 9, 8), grid_spacing=155e-9)
+    g[:, 4, 4] = fd.LineDetector(name="line")
+    g[2:4, 2:4, 2:4] = fd.BlockDetector(name="block")
+    g[:, :, 5] = fd.DFTPlaneDetector(frequencies=[1e14], name="dft")
+    with pytest.raises(Exception):
+        g.save_data()  # no folder yet, as in the reference
+    folder = g.save_simulation("keys")
+    g.save_data()
+    got = np.load(os.path.join(folder, "detector_readings.npz"))
+    assert set(got.files) == {"line (E)", "line (H)", "block (E)", "block (H)", "dft (dft)"}
+    assert got["line (E)"].shape == (0, 10, 3) and got["block (H)"].shape == (0, 3, 3, 3, 3)
+    assert got["dft (dft)"].shape == (1, 10, 9, 1, 3)

@@ -1,5 +1,7 @@
-"""bench.py's reference arm (the reference's numpy time step, restated, on
-the host cores) prints one JSON line with the contract's keys; no GPU needed."""
+"""bench.py's reference arm (the reference's own numpy time step on the host
+cores: the unmodified package in baseline/_ref, or the oracle port of it when
+that is not installed) prints one JSON line with the contract's keys; no GPU
+needed."""
 
 import json
 import os
@@ -10,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_json_line():
-    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "24",
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
                           "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
@@ -20,5 +22,7 @@ def test_reference_arm_json_line():
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in d, key
     assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == 1
+    installed = os.path.isfile(os.path.join(ROOT, "baseline", "_ref", "fdtd", "__init__.py"))
+    assert d["cpu_baseline"]["kind"] == ("reference" if installed else "port")
+    assert d["cpu_baseline"]["cores"] == 1 and d["config"]["sample_grid"] == [128, 128, 128]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]

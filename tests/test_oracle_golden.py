@@ -109,3 +109,32 @@ def test_oracle_matches_reference_on_random_scenes(seed):
             assert np.linalg.norm(a - b) <= 1e-14 * scale, k
         else:
             assert np.array_equal(a, b), k
+
+
+def test_oracle_config1_full_size_bit_identical():
+    """Config 1 at its full size and step count (64^3, 500 steps) against the
+    reference's own run: identical traces and planes, and identical SHA-256
+    digests of the whole final E and H (ref_c1_full.npz).  The digests pin
+    every bit on an x86 host like the one that made the fixture; a host whose
+    numpy exp rounds a PML coefficient differently still matches the planes
+    and traces to 1e-12."""
+    import hashlib
+    import platform
+
+    from fdtd_gb300 import scenes
+
+    fix = np.load(os.path.join(GOLDEN, "ref_c1_full.npz"))
+    g = scenes.c1(fo)
+    g.run(int(fix["steps"]))
+    E, H = np.ascontiguousarray(g.E, np.float64), np.ascontiguousarray(g.H, np.float64)
+    planes = list(fix["planes"])
+    d = g.detectors[0]
+    got = {"trace_E": np.stack(d.E), "trace_H": np.stack(d.H), "E_planes": E[planes], "H_planes": H[planes]}
+    if platform.machine() in ("x86_64", "AMD64"):
+        for key, val in got.items():
+            assert np.array_equal(val, fix[key]), key
+        assert hashlib.sha256(E.tobytes()).hexdigest() == str(fix["E_sha256"])
+        assert hashlib.sha256(H.tobytes()).hexdigest() == str(fix["H_sha256"])
+    else:
+        for key, val in got.items():
+            assert np.linalg.norm(val - fix[key]) <= 1e-12 * np.linalg.norm(fix[key]), key

@@ -332,3 +332,34 @@ def test_reset_keeps_plan(fd):
     assert g.time_steps_passed == 0 and float(g.E.abs().max()) == 0.0
     g.run(3, progress_bar=False)
     assert float(g.E.abs().max()) > 0.0
+
+
+@pytest.mark.parametrize("name", ["c2", "saps"])
+def test_save_data_matches_device_traces_and_reference(fd, name, tmp_path, monkeypatch):
+    """Grid.save_data (fdtd/grid.py:490-514): '<name> (E)' and '<name> (H)'
+    for every E/H detector, read from the device traces; the saved records
+    match the traces and the reference's own records of the scene.  A
+    CurrentDetector (on which the reference raises KeyError) stores
+    '<name> (I)'."""
+    monkeypatch.chdir(tmp_path)
+    fd.set_backend("gb300.float64")
+    grid, steps, drive = golden_scenes.SCENES[name](fd)
+    drive(grid, steps)
+    folder = grid.save_simulation("parity")
+    grid.save_data()
+    got = np.load(os.path.join(folder, "detector_readings.npz"))
+    want = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    keys = set()
+    for i, det in enumerate(grid.detectors):
+        if hasattr(det, "I"):
+            keys.add(f"{det.name} (I)")
+            assert np.array_equal(got[f"{det.name} (I)"], np.asarray(det.I))
+            assert rel_l2(got[f"{det.name} (I)"], want[f"det{i}_I"]) <= TOL64
+            continue
+        for f in ("E", "H"):
+            key = f"{det.name} ({f})"
+            keys.add(key)
+            assert np.array_equal(got[key], np.asarray(getattr(det, f)))
+            assert got[key].shape == want[f"det{i}_{f}"].shape
+            assert rel_l2(got[key], want[f"det{i}_{f}"]) <= TOL64
+    assert set(got.files) == keys
