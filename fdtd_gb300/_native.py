@@ -11,7 +11,7 @@ import os
 LIB_NAME = "libfdtd_gb300.so"
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), LIB_NAME)
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 MAX_BOUNDARIES = 9
 
 FLOAT32, FLOAT32C, FLOAT64 = 0, 1, 2
@@ -80,6 +80,9 @@ class GridDesc(ctypes.Structure):
         ("grid_spacing", ctypes.c_double), ("materials_scaled", c_int32),
         ("eps_table", c_void_p), ("n_eps_table", c_int32), ("eps_index", c_void_p),
         ("mu_table", c_void_p), ("n_mu_table", c_int32), ("mu_index", c_void_p),
+        ("step_fusion", c_int32), ("reserved_fusion", c_int32),
+        ("E_alt", c_void_p), ("H_alt", c_void_p),
+        ("psi_alt", (c_void_p * 2) * MAX_BOUNDARIES),
     ]
 
 
@@ -127,6 +130,8 @@ SIGNATURES = {
     "fdtd_field_stats": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "fdtd_field_stats_noalloc": (c_int32, [c_void_p, c_void_p, c_int32, c_void_p]),
     "fdtd_plan_tiling": (c_int32, [c_void_p, ctypes.POINTER(c_int64)]),
+    "fdtd_plan_step_fusion": (c_int32, [c_void_p, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32),
+                                        ctypes.POINTER(c_int32)]),
     "fdtd_status_string": (ctypes.c_char_p, [c_int32]),
     "fdtd_last_cuda_error": (c_int32, []),
     "fdtd_abi_sizeof": (ctypes.c_size_t, [c_int32]),

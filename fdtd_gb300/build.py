@@ -16,7 +16,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-SOURCES = ["fdtd_f32.cu", "fdtd_f64.cu", "fdtd_adjoint.cu", "fdtd_capi.cu"]
+SOURCES = ["fdtd_f32.cu", "fdtd_f64.cu", "fdtd_adjoint.cu", "fdtd_onepass.cu", "fdtd_capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"] + ARCH
 

@@ -67,27 +67,30 @@ struct Tiling {
     int V, TZ, TY, XC, gz, gy, gx;
 };
 
-static void cta_range(const Tiling &t, const int32_t lo[3], const int32_t hi[3], int r[6]) {
-    const int zc = t.V * t.TZ;
-    r[0] = lo[2] / zc;
+// With `halo`, a CTA also covers the cell past its tile along each axis (the
+// one-pass step recomputes the new E there), so an item starting at a tile's
+// first cell is listed for the tile before it as well.
+static void cta_range(const Tiling &t, const int32_t lo[3], const int32_t hi[3], int r[6], bool halo = false) {
+    const int zc = t.V * t.TZ, h = halo ? 1 : 0;
+    r[0] = std::max(0, lo[2] - h) / zc;
     r[1] = (hi[2] - 1) / zc;
-    r[2] = lo[1] / t.TY;
+    r[2] = std::max(0, lo[1] - h) / t.TY;
     r[3] = (hi[1] - 1) / t.TY;
-    r[4] = lo[0] / t.XC;
+    r[4] = std::max(0, lo[0] - h) / t.XC;
     r[5] = (hi[0] - 1) / t.XC;
 }
 
 // CSR lists: for every CTA, the indices (into the device item array) of the
-// items whose box intersects the CTA's cells, in item order.
+// items whose box intersects the CTA's cells (and its halo), in item order.
 static void build_csr(const Tiling &t, const std::vector<ItemK> &items, int first, int count,
-                      std::vector<int> &off, std::vector<int> &idx) {
+                      std::vector<int> &off, std::vector<int> &idx, bool halo = false) {
     const long ncta = (long)t.gz * t.gy * t.gx;
     off.assign(ncta + 1, 0);
     idx.clear();
     std::vector<int> cnt(ncta, 0);
     for (int q = first; q < first + count; ++q) {
         int r[6];
-        cta_range(t, items[q].lo, items[q].hi, r);
+        cta_range(t, items[q].lo, items[q].hi, r, halo);
         for (int cx = r[4]; cx <= r[5]; ++cx)
             for (int cy = r[2]; cy <= r[3]; ++cy)
                 for (int cz = r[0]; cz <= r[1]; ++cz) cnt[cz + t.gz * (cy + (long)t.gy * cx)]++;
@@ -97,7 +100,7 @@ static void build_csr(const Tiling &t, const std::vector<ItemK> &items, int firs
     std::vector<int> fill(off.begin(), off.end() - 1);
     for (int q = first; q < first + count; ++q) {
         int r[6];
-        cta_range(t, items[q].lo, items[q].hi, r);
+        cta_range(t, items[q].lo, items[q].hi, r, halo);
         for (int cx = r[4]; cx <= r[5]; ++cx)
             for (int cy = r[2]; cy <= r[3]; ++cy)
                 for (int cz = r[0]; cz <= r[1]; ++cz) idx[fill[cz + t.gz * (cy + (long)t.gy * cx)]++] = q;
@@ -200,6 +203,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             S.thp = bd.axis == 2 ? bd.thickness + (bd.thickness & 1) : bd.thickness;
             S.psiE = bd.psi_E;
             S.psiH = bd.psi_H;
+            S.psiE_rd = bd.psi_E;
+            S.psiH_rd = bd.psi_H;
             S.bE = bd.b_E;
             S.cE = bd.c_E;
             S.bH = bd.b_H;
@@ -627,6 +632,184 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     build_csr(t, items, srcE0, d->n_sources_E, se_off, se_idx);
     build_csr(t, items, srcH0, d->n_sources_H, sh_off, sh_idx);
 
+    // ---- one pass per time step (fdtd_onepass.cuh) ----
+    // Allowed for float32 plans whose every PML slab precedes any periodic
+    // boundary, with periodic boundaries only along x, no object or source on
+    // a periodic plane and no feedback source; used when the caller gave the
+    // second buffers and asked for it (or automatically from 8M cells).
+    if (d->step_fusion < 0 || d->step_fusion > 2) return FDTD_ERR_ARGUMENT;
+    p.onepass = p.onepass_ok = p.onepass_hcopy = p.onepass_why = 0;
+    GridK kl;  // tiling and stage layout of the one-pass kernel
+    memset(&kl, 0, sizeof(kl));
+    Tiling to{};
+    std::vector<int> oo_off, oo_idx, ose_off, ose_idx, osh_off, osh_idx;
+    {
+        int why = 0;  // first reason the grid does not allow it (fdtd_plan_step_fusion)
+        auto refuse = [&](int r) {
+            if (why == 0) why = r;
+        };
+        if (d->precision != FDTD_FLOAT32) refuse(1);
+        if (!vec) refuse(2);
+        if (p.has_feedback) refuse(3);
+        bool periodic_seen = false, per_x = false;
+        for (int b = 0; b < d->n_boundaries; ++b) {
+            const fdtd_boundary_desc &bd = d->boundaries[b];
+            if (bd.kind == FDTD_BOUNDARY_PERIODIC) {
+                if (n[bd.axis] <= 1) continue;  // a plane copied onto itself
+                if (bd.axis != 0 || per_x) refuse(5);
+                per_x = true;
+                periodic_seen = true;
+            } else if (periodic_seen) {
+                refuse(4);  // a PML slab after a periodic boundary
+            }
+        }
+        if (per_x && d->nx < 4) refuse(5);
+        if (per_x)
+            for (const ItemK &it : items)
+                if (it.lo[0] == 0 || it.hi[0] == d->nx) refuse(6);
+        const bool ok = why == 0;
+        p.onepass_ok = ok ? 1 : 0;
+        bool alt = d->E_alt != nullptr && d->H_alt != nullptr && aligned16(d->E_alt) && aligned16(d->H_alt);
+        for (int b = 0; b < d->n_boundaries; ++b)
+            if (d->boundaries[b].kind == FDTD_BOUNDARY_PML &&
+                (!d->psi_alt[b][0] || !d->psi_alt[b][1] || !aligned16(d->psi_alt[b][0]) ||
+                 !aligned16(d->psi_alt[b][1])))
+                alt = false;
+        const bool want = d->step_fusion == 2 || (d->step_fusion == 0 && ncell >= (8L << 20));
+        if (ok && !alt) refuse(7);
+        p.onepass_why = why;
+        if (want && ok && alt) {
+            const int V = PF32::V, Zc = 32 * V;
+            const int matE = mat_want[0], matH = mat_want[1] == MAT_IDS ? MAT_FULL : mat_want[1];
+            const int lut_rows = std::max(mat_lut_rows(matE), mat_lut_rows(matH));
+            int coef = 0;
+            for (int s = 0; s < g.nslab; ++s) {
+                kl.coef_off[s] = coef;
+                coef += 2 * g.slab[s].th;
+            }
+            kl.coef_values = (size_t)coef * esize <= 16384 ? coef : 0;
+            // stage layout of a tile height: field tiles, then per group of slabs of
+            // one axis that never meet in one stage an E-side slot (TY+1 rows;
+            // x/y slabs Zc+2 pairs) and an H-side slot (TY rows)
+            auto layout = [&](int TY) -> size_t {
+                size_t stage = onepass_bytes(d->precision, TY, matE, matH, 0);
+                struct Slot {
+                    int axis;
+                    size_t bE, bH, offE, offH;
+                    std::vector<std::pair<int, int>> ranges;
+                };
+                std::vector<Slot> slots;
+                int slot_of[kMaxSlabs] = {0};
+                for (int s = 0; s < g.nslab; ++s) {
+                    const SlabK &S = g.slab[s];
+                    const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? TY : Zc);
+                    const int lo = S.axis == 0 ? S.start : std::max(0, S.start - 1);  // tiles whose halo reaches it
+                    const std::pair<int, int> rg(lo / unit, (S.start + S.th - 1) / unit);
+                    const int pE = S.axis == 2 ? 2 * S.thp : 2 * (Zc + 2);
+                    const int pH = S.axis == 2 ? 2 * S.thp : 2 * Zc;
+                    kl.psi_pitch[s] = pE;
+                    kl.psi_pitchH[s] = pH;
+                    const size_t bE = (size_t)(TY + 1) * pE * esize, bH = (size_t)TY * pH * esize;
+                    int found = -1;
+                    for (int q = 0; q < (int)slots.size() && found < 0; ++q) {
+                        if (slots[q].axis != S.axis) continue;
+                        bool disjoint = true;
+                        for (auto &o : slots[q].ranges)
+                            if (!(rg.second < o.first || o.second < rg.first)) disjoint = false;
+                        if (disjoint) found = q;
+                    }
+                    if (found < 0) {
+                        slots.push_back(Slot{S.axis, 0, 0, 0, 0, {}});
+                        found = (int)slots.size() - 1;
+                    }
+                    slots[found].ranges.push_back(rg);
+                    slots[found].bE = std::max(slots[found].bE, bE);
+                    slots[found].bH = std::max(slots[found].bH, bH);
+                    slot_of[s] = found;
+                }
+                for (auto &sl : slots) {
+                    sl.offE = stage;
+                    stage += (sl.bE + 127) & ~(size_t)127;
+                    sl.offH = stage;
+                    stage += (sl.bH + 127) & ~(size_t)127;
+                }
+                for (int s = 0; s < g.nslab; ++s) {
+                    kl.psi_off[s] = (int)slots[slot_of[s]].offE;
+                    kl.psi_offH[s] = (int)slots[slot_of[s]].offH;
+                }
+                return stage;
+            };
+            const size_t extra = 2 * (size_t)kl.coef_values * esize + (matE != MAT_FULL ? 16 * (size_t)lut_rows : 0) +
+                                 (matH != MAT_FULL ? 16 * (size_t)lut_rows : 0) + 16 + 128;
+            const long per_sm = 228L * 1024;
+            auto smem_of = [&](int TY, size_t stage, int S) {
+                return (size_t)S * stage + (size_t)S * 8 + 2 * onepass_bytes(d->precision, TY, matE, matH, 1) + extra;
+            };
+            // tile height and ring depth: two CTAs per SM with at least three
+            // stages where that fits, else one CTA with up to six stages
+            int TY = (d->tile_rows == 4 || d->tile_rows == 8) ? d->tile_rows : 0;
+            int S = d->stages >= 3 ? d->stages : 0;
+            auto fit_two = [&](int ty) {
+                const size_t st = layout(ty);
+                for (int q = 6; q >= 3; --q)
+                    if ((long)smem_of(ty, st, q) + 1024 <= per_sm / 2 && smem_of(ty, st, q) <= (size_t)optin) return q;
+                return 0;
+            };
+            if (TY == 0) TY = fit_two(8) ? 8 : 4;
+            const size_t stage = layout(TY);
+            if (S == 0) {
+                S = fit_two(TY);
+                if (S == 0)
+                    for (int q = 6; q >= 3 && S == 0; --q)
+                        if (smem_of(TY, stage, q) <= (size_t)optin) S = q;
+            }
+            const size_t smem = S >= 3 ? smem_of(TY, stage, S) : 0;
+            if (S < 3 || smem > (size_t)optin) {
+                p.onepass_why = 8;
+            } else {
+                const int ctas = std::max(1, (int)(per_sm / (long)(smem + 1024)));
+                to.V = V;
+                to.TZ = 32;
+                to.TY = TY;
+                to.gz = (d->nz + Zc - 1) / Zc;
+                to.gy = (d->ny + TY - 1) / TY;
+                if (d->x_chunk > 0) {
+                    to.XC = d->x_chunk;
+                } else {
+                    // about forty waves of CTAs (a short last wave), at least 32
+                    // planes per chunk (a chunk stages one plane before it and
+                    // recomputes one after it)
+                    const long cols = (long)to.gz * to.gy, wave = (long)n_sm * ctas;
+                    long chunks = (40L * wave + cols - 1) / cols;
+                    chunks = std::max(1L, std::min(chunks, std::max(1L, (long)d->nx / 32)));
+                    to.XC = (int)((d->nx + chunks - 1) / chunks);
+                }
+                to.gx = (d->nx + to.XC - 1) / to.XC;
+                if (to.gy <= 65535 && to.gx <= 65535) {
+                    kl.TZ = 32;
+                    kl.TY = TY;
+                    kl.XC = to.XC;
+                    kl.stages = S;
+                    kl.stage_bytes = (int)stage;
+                    kl.lut_rows = lut_rows;
+                    kl.mat_E = matE;
+                    kl.mat_H = matH;
+                    kl.periodic_x = per_x ? 1 : 0;
+                    p.osmem = smem;
+                    p.ogrid = dim3(to.gz, to.gy, to.gx);
+                    p.oblock = dim3(32, TY + 1, 1);
+                    p.onepass = 1;
+                    p.onepass_hcopy = per_x ? 1 : 0;
+                    build_csr(to, items, 0, srcE0, oo_off, oo_idx, true);
+                    build_csr(to, items, srcE0, d->n_sources_E, ose_off, ose_idx, true);
+                    build_csr(to, items, srcH0, d->n_sources_H, osh_off, osh_idx, true);
+                } else {
+                    p.onepass_why = 9;
+                }
+            }
+        }
+    }
+
     // probes, current probes and DFT boxes
     p.n_probe = d->n_probe_cells;
     p.probe_cells = d->probe_cells;
@@ -648,7 +831,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t b_items = align(sizeof(ItemK) * std::max(1, nitems));
     const size_t b_lists = align(sizeof(int) * (obj_off.size() + obj_idx.size() + se_off.size() + se_idx.size() +
-                                                sh_off.size() + sh_idx.size() + 6));
+                                                sh_off.size() + sh_idx.size() + oo_off.size() + oo_idx.size() +
+                                                ose_off.size() + ose_idx.size() + osh_off.size() + osh_idx.size() +
+                                                12));
     const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
     const size_t b_status = 256;
     std::vector<char> host(b_items + b_lists + b_runs + b_status, 0);
@@ -667,6 +852,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     put(se_idx, at_se_idx);
     put(sh_off, at_sh_off);
     put(sh_idx, at_sh_idx);
+    size_t at_oo_off, at_oo_idx, at_ose_off, at_ose_idx, at_osh_off, at_osh_idx;
+    put(oo_off, at_oo_off);
+    put(oo_idx, at_oo_idx);
+    put(ose_off, at_ose_off);
+    put(ose_idx, at_ose_idx);
+    put(osh_off, at_osh_off);
+    put(osh_idx, at_osh_idx);
     if (!runs.empty()) memcpy(host.data() + b_items + b_lists, runs.data(), sizeof(int2) * runs.size());
     ce = cudaMalloc(&p.dev_mem, host.size());
     if (ce != cudaSuccess) return cuda_fail(ce);
@@ -698,6 +890,65 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (p.pml_split) {
         p.kf.nslab = p.fused_slabs;
         p.kf.nslab_fused = p.fused_slabs;
+    }
+
+    if (p.onepass) {
+        // direction 0 reads the caller's buffers and writes the alternates,
+        // direction 1 the reverse; every slab is handled inside the pass
+        for (int dir = 0; dir < 2; ++dir) {
+            GridK &k = p.ko[dir];
+            k = p.k;
+            k.nslab_fused = k.nslab;
+            k.TZ = kl.TZ;
+            k.TY = kl.TY;
+            k.XC = kl.XC;
+            k.stages = kl.stages;
+            k.stage_bytes = kl.stage_bytes;
+            for (int s = 0; s < kMaxSlabs; ++s) {
+                k.psi_off[s] = kl.psi_off[s];
+                k.psi_pitch[s] = kl.psi_pitch[s];
+                k.psi_offH[s] = kl.psi_offH[s];
+                k.psi_pitchH[s] = kl.psi_pitchH[s];
+                k.coef_off[s] = kl.coef_off[s];
+            }
+            k.coef_values = kl.coef_values;
+            k.lut_rows = kl.lut_rows;
+            k.mat_E = kl.mat_E;
+            k.mat_H = kl.mat_H;
+            k.mlut_E = d->eps_table;
+            k.mlut_H = d->mu_table;
+            k.nlut_E = kl.mat_E == MAT_FULL ? 0 : d->n_eps_table;
+            k.nlut_H = kl.mat_H == MAT_FULL ? 0 : d->n_mu_table;
+            k.mid_E = kl.mat_E == MAT_IDS ? d->eps_index : nullptr;
+            k.mid_H = nullptr;
+            k.periodic_x = kl.periodic_x;
+            k.obj_off = dl + at_oo_off;
+            k.obj_idx = dl + at_oo_idx;
+            k.srcE_off = dl + at_ose_off;
+            k.srcE_idx = dl + at_ose_idx;
+            k.srcH_off = dl + at_osh_off;
+            k.srcH_idx = dl + at_osh_idx;
+            k.fuse_src_E = k.fuse_src_H = 1;
+            void *Ea = d->E, *Ha = d->H, *Eb = d->E_alt, *Hb = d->H_alt;
+            k.E = dir == 0 ? Eb : Ea;  // written
+            k.H = dir == 0 ? Hb : Ha;
+            for (int s = 0; s < k.nslab; ++s) {
+                const int b = p.slab_boundary[s];
+                void *pa_E = d->boundaries[b].psi_E, *pa_H = d->boundaries[b].psi_H;
+                void *pb_E = d->psi_alt[b][0], *pb_H = d->psi_alt[b][1];
+                k.slab[s].psiE = dir == 0 ? pb_E : pa_E;
+                k.slab[s].psiH = dir == 0 ? pb_H : pa_H;
+                k.slab[s].psiE_rd = dir == 0 ? pa_E : pb_E;
+                k.slab[s].psiH_rd = dir == 0 ? pa_H : pb_H;
+            }
+        }
+        const int rc = prepare_onepass_f32(p);
+        if (rc == FDTD_ERR_UNSUPPORTED) {
+            p.onepass = 0;  // a tensor map the one-pass kernel needs was refused
+            p.onepass_why = 10;
+        } else if (rc != FDTD_OK) {
+            return rc;
+        }
     }
 
     p.stats_ctas = std::max(1, std::min(4 * n_sm, FDTD_STATS_STATIC_MAX_ROWS));
@@ -974,9 +1225,28 @@ int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_row
     return e == cudaSuccess ? FDTD_OK : cuda_fail(e);
 }
 
+int fdtd_plan_step_fusion(const fdtd_plan *plan, int32_t *allowed, int32_t *active, int32_t *reason) {
+    if (!plan || !allowed || !active) return FDTD_ERR_ARGUMENT;
+    *allowed = plan->p.onepass_ok;
+    *active = plan->p.onepass;
+    if (reason) *reason = plan->p.onepass ? 0 : plan->p.onepass_why;
+    return FDTD_OK;
+}
+
 int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8) {
     if (!plan || !out8) return FDTD_ERR_ARGUMENT;
     const Plan &p = plan->p;
+    if (p.onepass) {  // full steps run as one pass each
+        out8[0] = PF32::V;
+        out8[1] = 32;
+        out8[2] = p.ko[0].TY;
+        out8[3] = p.ko[0].XC;
+        out8[4] = (int64_t)p.ogrid.x * p.ogrid.y * p.ogrid.z;
+        out8[5] = 1 + p.onepass_hcopy + (p.n_probe > 0 ? 2 : 0) + (p.n_current > 0 ? 1 : 0) + (int64_t)p.dft.size();
+        out8[6] = 4;
+        out8[7] = p.ko[0].stages;
+        return FDTD_OK;
+    }
     out8[0] = p.V;
     out8[1] = p.k.TZ;
     out8[2] = p.k.TY;

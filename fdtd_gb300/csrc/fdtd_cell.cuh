@@ -207,12 +207,15 @@ __device__ __forceinline__ void pml_correct(typename P::T &f, typename P::T &fl,
 // (dx F_y, dx F_z, dy F_x, dy F_z, dz F_x, dz F_y); a slab normal to axis a
 // drives its pair with (dF_(a+2)%3, dF_(a+1)%3) along a.  IS_E selects the E
 // rule (increment at slab-local index >= 1, E += c m phi) or the H rule
-// (index <= th-2, H -= c m phi).
-template <class P, int V, bool IS_E>
+// (index <= th-2, H -= c m phi).  store = false computes without writing the
+// updated auxiliaries (a neighbour's cell recomputed by the one-pass step);
+// HOFF selects the stage's H-side auxiliary slots (g.psi_offH/psi_pitchH) of
+// the one-pass step instead of g.psi_off/psi_pitch.
+template <class P, int V, bool IS_E, bool HOFF = false>
 __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, typename P::T c,
                                           const typename P::T (&d)[6][V], const typename P::T (&m)[3 * V],
                                           typename P::T (&f)[3 * V], typename P::T (&fl)[3 * V],
-                                          const PsiSrc<typename P::T> &src, unsigned slabs) {
+                                          const PsiSrc<typename P::T> &src, unsigned slabs, bool store = true) {
     using T = typename P::T;
     for (unsigned sm = slabs; sm; sm &= sm - 1) {
         const int s = __ffs(sm) - 1;
@@ -230,8 +233,8 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
         T *gp = psi + 2 * gofs;
         const T *sp = nullptr;
         if (src.stage)
-            sp = reinterpret_cast<const T *>(src.stage + g.psi_off[s]) + src.row * g.psi_pitch[s] +
-                 (a == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
+            sp = reinterpret_cast<const T *>(src.stage + (HOFF ? g.psi_offH[s] : g.psi_off[s])) +
+                 src.row * (HOFF ? g.psi_pitchH[s] : g.psi_pitch[s]) + (a == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
         T bu = T(0), cu = T(0);  // coefficients when l is the same for the V cells
         if (a != 2) {
             bu = src.ctab ? src.ctab[g.coef_off[s] + l0] : bt[l0];
@@ -300,7 +303,8 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
                 }
             }
         }
-        if (V > 1 && a != 2) {
+        if (!store) {
+        } else if (V > 1 && a != 2) {
             alignas(16) T pr[2 * V];
 #pragma unroll
             for (int v = 0; v < V; ++v) {
@@ -321,14 +325,16 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
 }
 
 // E half step of a thread's V cells at (i, j, k0..k0+V-1).  hc: H of the cells,
-// hp: H at plane i-1, hj: H at row j-1, (kx, ky): Hx, Hy at k0-1.
-template <class P, int V>
+// hp: H at plane i-1, hj: H at row j-1, (kx, ky): Hx, Hy at k0-1.  store and
+// HOFF as for apply_pml.
+template <class P, int V, bool HOFF = false>
 __device__ __forceinline__ void thread_E(const GridK &g, const double *__restrict__ wave, int i, int j, int k0,
                                          typename P::T c, const typename P::T (&hc)[3 * V],
                                          const typename P::T (&hp)[3 * V], const typename P::T (&hj)[3 * V],
                                          typename P::T kx, typename P::T ky, const typename P::T (&m)[3 * V],
                                          typename P::T (&e)[3 * V], typename P::T (&el)[3 * V], int ob0, int ob1,
-                                         int sb0, int sb1, const PsiSrc<typename P::T> &src, unsigned slabs) {
+                                         int sb0, int sb1, const PsiSrc<typename P::T> &src, unsigned slabs,
+                                         bool store = true) {
     using T = typename P::T;
     T d[6][V];  // dxHy, dxHz, dyHx, dyHz, dzHx, dzHy (backward, zero on the first plane)
     T cu[3][V];  // curl H
@@ -352,7 +358,7 @@ __device__ __forceinline__ void thread_E(const GridK &g, const double *__restric
         P::add_prod(e[3 * v + 2], el[3 * v + 2], P::cm(c, m[3 * v + 2]), cu[2][v]);
     }
     if (ob0 < ob1) apply_objects_v<P, V>(g, i, j, k0, c, cu, e, el, ob0, ob1);
-    if (slabs) apply_pml<P, V, true>(g, i, j, k0, c, d, m, e, el, src, slabs);
+    if (slabs) apply_pml<P, V, true, HOFF>(g, i, j, k0, c, d, m, e, el, src, slabs, store);
 #pragma unroll
     for (int v = 0; v < V; ++v) {
         if (sb0 < sb1)
@@ -365,14 +371,14 @@ __device__ __forceinline__ void thread_E(const GridK &g, const double *__restric
 }
 
 // H half step of a thread's V cells.  ec: E of the cells, en: E at plane i+1,
-// ej: E at row j+1, (kx, ky): Ex, Ey at k0+V.
-template <class P, int V>
+// ej: E at row j+1, (kx, ky): Ex, Ey at k0+V.  store and HOFF as for apply_pml.
+template <class P, int V, bool HOFF = false>
 __device__ __forceinline__ void thread_H(const GridK &g, const double *__restrict__ wave, int i, int j, int k0,
                                          typename P::T c, const typename P::T (&ec)[3 * V],
                                          const typename P::T (&en)[3 * V], const typename P::T (&ej)[3 * V],
                                          typename P::T kx, typename P::T ky, const typename P::T (&m)[3 * V],
                                          typename P::T (&h)[3 * V], typename P::T (&hl)[3 * V], int sb0, int sb1,
-                                         const PsiSrc<typename P::T> &src, unsigned slabs) {
+                                         const PsiSrc<typename P::T> &src, unsigned slabs, bool store = true) {
     using T = typename P::T;
     T d[6][V];  // dxEy, dxEz, dyEx, dyEz, dzEx, dzEy (forward, zero on the last plane)
 #pragma unroll
@@ -391,7 +397,7 @@ __device__ __forceinline__ void thread_H(const GridK &g, const double *__restric
         P::sub_prod(h[3 * v + 1], hl[3 * v + 1], P::cm(c, m[3 * v + 1]), d[4][v] - d[1][v]);
         P::sub_prod(h[3 * v + 2], hl[3 * v + 2], P::cm(c, m[3 * v + 2]), d[0][v] - d[2][v]);
     }
-    if (slabs) apply_pml<P, V, false>(g, i, j, k0, c, d, m, h, hl, src, slabs);
+    if (slabs) apply_pml<P, V, false, HOFF>(g, i, j, k0, c, d, m, h, hl, src, slabs, store);
 #pragma unroll
     for (int v = 0; v < V; ++v) {
         if (sb0 < sb1)

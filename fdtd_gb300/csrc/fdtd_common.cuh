@@ -24,6 +24,9 @@ struct SlabK {
     int thp;  // stored slab-local extent: th, padded to even for z slabs
     void *psiE, *psiH;
     const void *bE, *cE, *bH, *cH;
+    // where the staged passes read the auxiliaries from: psiE / psiH, or the
+    // other buffer of the pair in a one-pass step (which writes psiE / psiH)
+    const void *psiE_rd, *psiH_rd;
 };
 
 // An object or source box on the device.  bny/bnz are the box extents used
@@ -65,6 +68,8 @@ struct GridK {
     // stage) and row pitch (values) of its psi slot
     int stage_bytes;
     int psi_off[kMaxSlabs], psi_pitch[kMaxSlabs];
+    // one-pass step: offset and row pitch of each slab's H-side auxiliary slot
+    int psi_offH[kMaxSlabs], psi_pitchH[kMaxSlabs];
     int coef_off[kMaxSlabs];  // per slab: offset (values) of its b/c tables in shared memory
     int coef_values;          // values of all staged b/c tables (0: tables are read from global)
     int scaled;               // ie / imu hold courant * inverse material (float64 plans)
@@ -75,6 +80,7 @@ struct GridK {
     int nlut_E, nlut_H;
     int lut_rows;  // padded 4-value rows reserved for the table in shared memory
     const unsigned char *mid_E, *mid_H;  // one-byte material indices (MAT_IDS)
+    int periodic_x;  // one-pass step: a periodic boundary along x follows the PML slabs
 };
 
 template <class T>

@@ -3,6 +3,8 @@
 
 #include <cudaTypedefs.h>
 
+#include <type_traits>
+
 #include "fdtd_adjoint.cuh"
 #include "fdtd_kernels.cuh"
 #include "fdtd_plan.hpp"
@@ -293,8 +295,38 @@ static int run_impl(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *ca
     }
     const GridK &g = p.k;
     const int pblocks = (3 * p.n_probe + kThreads - 1) / kThreads;
+    // one pass per full step (float32 plans that have it), in pairs: the first
+    // pass of a pair writes the alternate buffers, the second the caller's; an
+    // odd last step runs the two passes
+    int64_t nfused = 0;
+    if constexpr (std::is_same<P, PF32>::value) {
+        if (p.onepass && a->half == 0 && cap == nullptr) nfused = a->n_steps & ~(int64_t)1;
+    }
     for (int64_t s = 0; s < a->n_steps; ++s) {
         const double *wave = p.n_columns > 0 ? a->wave + s * p.n_columns : nullptr;
+        if (s < nfused) {
+            const int dir = (int)(s & 1);
+            const GridK &ko = p.ko[dir];
+            onepass_step_f32(p, dir, wave, st);
+            if (probe) {
+                k_probe<T><<<pblocks, kThreads, 0, st>>>((const T *)ko.E, p.probe_cells, p.n_probe,
+                                                        (T *)a->trace_E + (a->record_E + s) * 3 * p.n_probe);
+                k_probe<T><<<pblocks, kThreads, 0, st>>>((const T *)ko.H, p.probe_cells, p.n_probe,
+                                                        (T *)a->trace_H + (a->record_H + s) * 3 * p.n_probe);
+            }
+            for (const fdtd_dft_desc &d : p.dft) {
+                const long cells = (long)(d.hi[0] - d.lo[0]) * (d.hi[1] - d.lo[1]) * (d.hi[2] - d.lo[2]);
+                k_dft<T, P::COMP><<<grid_stride_blocks(cells * 3), kThreads, 0, st>>>(
+                    (const T *)ko.E, (const T *)g.Elo, g.ny, g.nz, d, a->phase + s * 2 * p.n_phase_columns);
+            }
+            if (current)
+                k_current<T><<<(p.n_current + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+                    (const T *)ko.H, p.current_cells, p.n_current, g.nx, g.ny, g.nz, p.grid_spacing,
+                    (T *)a->trace_I + (a->record_I + s) * p.n_current);
+            const int rc = check_launch<P>();
+            if (rc != FDTD_OK) return rc;
+            continue;
+        }
         if (cap != nullptr) {
             for (int q = 0; q < cap->n_curl; ++q) {
                 if (cap->curl[q] == nullptr) continue;

@@ -62,6 +62,16 @@ struct Plan {
     int n_objects, srcE0, n_srcE, srcH0, n_srcH;
     int slab_boundary[kMaxSlabs];
     std::vector<EpiOp> adj_E, adj_H;
+    // one pass per time step (fused E and H half steps on double-buffered
+    // state): whether the grid allows it, whether full steps use it (and why
+    // not), the periodic H copy it needs after each pass, the GridK of each
+    // direction (0: caller buffers -> alternates, 1: back), their tensor maps
+    // (H source, E source, E material, H material) and the launch shape
+    int onepass_ok, onepass, onepass_hcopy, onepass_why;
+    GridK ko[2];
+    CUtensorMap omaps[2][4];
+    dim3 ogrid, oblock;
+    size_t osmem;
 };
 
 // Per-precision entry points (one translation unit per precision).  `cap`
@@ -85,6 +95,13 @@ int prepare_tma_f32c(Plan &p);
 int prepare_tma_f64(Plan &p);
 
 void set_last_cuda_error(int e);
+
+// One-pass step (float32): tensor maps and shared-memory attribute; the pass
+// of one direction; bytes of the field part of a stage (what = 0) or of one
+// new-E exchange slot (what = 1) for a tile height and the material modes.
+int prepare_onepass_f32(Plan &p);
+int onepass_step_f32(Plan &p, int dir, const double *wave, cudaStream_t st);
+size_t onepass_bytes(int precision, int tile_rows, int mat_E, int mat_H, int what);
 
 inline int grid_stride_blocks(long total) {
     long b = (total + kThreads - 1) / kThreads;

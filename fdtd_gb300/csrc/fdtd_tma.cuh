@@ -129,7 +129,7 @@ __device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, ui
         const int j = j0 + rr;
         if (!with_psi || s >= g.nslab || j >= g.ny) continue;
         const SlabK &S = g.slab[s];
-        const T *psi = (const T *)(is_E ? S.psiE : S.psiH);
+        const T *psi = (const T *)(is_E ? S.psiE_rd : S.psiH_rd);
         const int cells = min(Zc, g.nz - k0c);
         size_t off;
         uint32_t nb;

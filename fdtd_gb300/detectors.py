@@ -62,6 +62,14 @@ class TraceList(collections.abc.Sequence):
             return torch.zeros((0,) + self._det._rec_shape)
         return chunks[0].clone() if len(chunks) == 1 else torch.cat(chunks, 0)
 
+    def tensor_tail(self, n):
+        """The last n records as one tensor: a view of the device trace buffer
+        when they were all written since the last plan rebuild."""
+        chunks = self._chunks()
+        if chunks and chunks[-1].shape[0] >= n:
+            return chunks[-1][chunks[-1].shape[0] - n:]
+        return self.tensor()[len(self) - n:]
+
     def numpy(self):
         return self.tensor().detach().cpu().numpy()
 

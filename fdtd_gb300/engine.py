@@ -139,6 +139,16 @@ def compact_material(x, chunk=1 << 25, index_ok=True):
     return table, index.reshape(x.shape[:-1])
 
 
+_FUSION_REASONS = {
+    1: "float32 plans only", 2: "nz must be a multiple of 4 (and the buffers 16-byte aligned)",
+    3: "a SoftArbitraryPointSource", 4: "a PML registered after a periodic boundary",
+    5: "a periodic boundary not along x (or fewer than 4 planes along x)",
+    6: "an object or source on a periodic plane", 7: "the second buffers could not be allocated",
+    8: "too little shared memory for the stages", 9: "the grid is too large for the launch",
+    10: "a tensor map was refused",
+}
+
+
 class _PinnedStager:
     """Double-buffered pinned host staging for small per-call tables."""
 
@@ -174,7 +184,9 @@ class Engine:
         self.x_chunk = x_chunk
         # fused-pass kernel choice: variant 0 auto / 1 register streaming / 2 TMA-staged
         # materials: 0 compact copies for the staged passes where possible, 1 full arrays only
-        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0, "materials": 0}
+        # step_fusion: 0 auto / 1 two passes per step / 2 one pass per step (where allowed)
+        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0, "materials": 0, "step_fusion": 0}
+        self._alt = None  # second buffers of E, H and the PML auxiliaries for one-pass steps
         self.plan = None
         self._key = None
         self._keep = []
@@ -272,7 +284,7 @@ class Engine:
         """How the plan's staged passes read each material (inverse permittivity,
         inverse permeability): None (full arrays; always for the register
         kernels), ("uniform", 1) or ("index", n distinct value triples)."""
-        if self.plan is None or self.tiling()["variant"] != 2:
+        if self.plan is None or self.tiling()["variant"] not in (2, 4):
             return [None, None]
         return [None if e is None else (("index", e[0].shape[0]) if e[1] is not None else ("uniform", 1))
                 for e in self._compact]
@@ -281,17 +293,22 @@ class Engine:
         self.x_chunk = int(x_chunk)
         self.refresh()
 
-    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None, materials=None):
+    def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None, materials=None,
+                   step_fusion=None):
         """Choose the fused-pass kernels (0 auto, 1 register streaming, 2 TMA-staged),
         the TMA tile rows (4 or 8 with 32-thread-wide tiles, 16 with 16-wide) and
         ring stages, where the PML slabs run
         (0 auto, 1 inside the fused pass, 2 kernels of their own; 3 only the
-        leading x/y slabs split off), and how the staged passes read the
+        leading x/y slabs split off), how the staged passes read the
         materials (0 a one-byte index into a table of distinct value triples,
         or nothing for a uniform material, where the materials allow; 1 the
-        full arrays); 0 keeps the automatic choice."""
+        full arrays), and whether full steps run as one pass each (0 auto:
+        float32 grids of 8M cells or more that allow it; 1 never; 2 always
+        where the grid allows it, else RuntimeError); 0 keeps the automatic
+        choice.  The one-pass step uses tile_rows 4 or 8, stages >= 3 and
+        x_chunk when given."""
         for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode),
-                     ("materials", materials)):
+                     ("materials", materials), ("step_fusion", step_fusion)):
             if v is not None:
                 self.tuning[k] = int(v)
         if x_chunk is not None:
@@ -494,11 +511,85 @@ class Engine:
         keep.extend([arrE, arrH])
 
 
+        # one pass per step: the library decides whether the grid allows it;
+        # the second buffers it needs are allocated only when it will be used
+        # (float32 grids of 8M cells or more, or when asked)
+        req = self.tuning["step_fusion"]
+        if self._alt is not None and (req == 1 or not self._alt_fits()):
+            self._alt = None
+        if self._alt is not None:
+            self._set_alt(d)
+            d.step_fusion = req
+        else:
+            d.step_fusion = 1 if req == 2 else req  # without the buffers: only ask whether it is allowed
         plan = ctypes.c_void_p()
         _native.check(lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan)), "fdtd_plan_create")
+        allowed, active, why = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+        _native.check(lib.fdtd_plan_step_fusion(plan, ctypes.byref(allowed), ctypes.byref(active), ctypes.byref(why)),
+                      "fdtd_plan_step_fusion")
+        ncell = g.Nx * g.Ny * g.Nz
+        want = req == 2 or (req == 0 and g.precision == "float32" and ncell >= (8 << 20))
+        if allowed.value and want and not active.value and self._alt is None:
+            try:
+                self._alloc_alt()
+            except torch.cuda.OutOfMemoryError:
+                self._alt = None
+            if self._alt is not None:
+                lib.fdtd_plan_destroy(plan)
+                self._set_alt(d)
+                d.step_fusion = req
+                plan = ctypes.c_void_p()
+                _native.check(lib.fdtd_plan_create(ctypes.byref(d), ctypes.byref(plan)), "fdtd_plan_create")
+                _native.check(lib.fdtd_plan_step_fusion(plan, ctypes.byref(allowed), ctypes.byref(active),
+                                                        ctypes.byref(why)), "fdtd_plan_step_fusion")
+        if req == 2 and not active.value:
+            lib.fdtd_plan_destroy(plan)
+            self._alt = None
+            raise RuntimeError(f"one pass per time step (step_fusion=2) is not possible here: "
+                               f"{_FUSION_REASONS.get(why.value, why.value)}")
+        if not active.value:
+            self._alt = None
         self.plan = plan
         self._keep = keep
         self.launches_per_step = self.tiling()["launches_per_step"]
+
+    # --- one pass per step: second buffers -----------------------------------------
+    def _alt_shapes(self):
+        g = self.grid
+        shapes = [tuple(g._E.shape), tuple(g._H.shape)]
+        for b in g.boundaries:
+            if isinstance(b, PML):
+                shapes += [tuple(b._psi_E.shape), tuple(b._psi_H.shape)]
+        return shapes
+
+    def _alt_fits(self):
+        return [tuple(t.shape) for t in self._alt] == self._alt_shapes() and self._alt[0].dtype == self.grid._dtype
+
+    def _alloc_alt(self):
+        g = self.grid
+        alt = [torch.empty_like(g._E), torch.empty_like(g._H)]
+        for b in g.boundaries:
+            if isinstance(b, PML):
+                alt += [torch.empty_like(b._psi_E), torch.empty_like(b._psi_H)]
+        self._alt = alt
+
+    def _set_alt(self, d):
+        g = self.grid
+        d.E_alt, d.H_alt = self._alt[0].data_ptr(), self._alt[1].data_ptr()
+        q = 2
+        for i, b in enumerate(g.boundaries):
+            if isinstance(b, PML):
+                d.psi_alt[i][0] = self._alt[q].data_ptr()
+                d.psi_alt[i][1] = self._alt[q + 1].data_ptr()
+                q += 2
+
+    def step_fusion(self):
+        """(allowed, active): whether this grid admits one pass per time step
+        and whether its full steps run that way."""
+        allowed, active = ctypes.c_int32(0), ctypes.c_int32(0)
+        _native.check(_native.load().fdtd_plan_step_fusion(self.plan, ctypes.byref(allowed), ctypes.byref(active),
+                                                            None), "fdtd_plan_step_fusion")
+        return bool(allowed.value), bool(active.value)
 
     # --- traces ---------------------------------------------------------------
     def _ensure_capacity(self, need):

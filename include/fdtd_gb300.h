@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 4
+#define FDTD_ABI_VERSION 5
 #define FDTD_MAX_BOUNDARIES 9 /* six PML slabs and three periodic axes */
 
 typedef void *fdtd_stream_t; /* a cudaStream_t */
@@ -186,6 +186,25 @@ typedef struct {
     const void *mu_table;
     int32_t n_mu_table;
     const uint8_t *mu_index;
+    /* One pass per time step (ABI 5).  The E and H half steps of a full step
+     * run as one TMA-staged pass that reads E, H, the PML auxiliaries and the
+     * materials once and writes E, H and the auxiliaries once; it reads the
+     * old values from one copy and writes the new ones to another, so the
+     * caller provides a second buffer of the same size for E, H and every PML
+     * auxiliary array (contents ignored).  Steps run in pairs that end in the
+     * caller's own buffers; an odd last step, single half steps and
+     * fdtd_run_capture use the two-pass kernels.  Float32 plans whose PML
+     * slabs all precede any periodic boundary, with periodic boundaries only
+     * along x, no object or source on a periodic plane, and without a
+     * feedback source.  step_fusion: 0 automatic (float32 grids of 8M cells
+     * or more when the buffers are given), 1 off, 2 on where the grid allows
+     * it.  fdtd_plan_step_fusion reports whether a grid allows it (before any
+     * buffer is allocated), whether the plan uses it, and why not. */
+    int32_t step_fusion;
+    int32_t reserved_fusion;
+    void *E_alt;
+    void *H_alt;
+    void *psi_alt[FDTD_MAX_BOUNDARIES][2]; /* per PML boundary: second psi_E, psi_H; NULL for periodic */
 } fdtd_grid_desc;
 
 typedef struct fdtd_plan fdtd_plan;
@@ -335,10 +354,22 @@ int fdtd_field_stats(const fdtd_plan *plan, double *stats, void *scratch, fdtd_s
 #define FDTD_STATS_STATIC_MAX_ROWS 1024
 int fdtd_field_stats_noalloc(const fdtd_plan *plan, double *stats, int32_t n_rows, fdtd_stream_t stream);
 
+/* One pass per time step: *allowed = 1 when the grid admits it (whether or
+ * not the second buffers were given), *active = 1 when full steps of this
+ * plan run as one pass each; *reason (may be NULL) says why not: 0 active
+ * or not asked, 1 not float32, 2 nz not a multiple of 4 or an unaligned
+ * buffer, 3 a feedback source, 4 a PML slab after a periodic boundary,
+ * 5 a periodic boundary not along x (or nx < 4), 6 an object or source on a
+ * periodic plane, 7 no second buffers, 8 too little shared memory, 9 grid
+ * too large for the launch, 10 a tensor map was refused.  No reference
+ * counterpart. */
+int fdtd_plan_step_fusion(const fdtd_plan *plan, int32_t *allowed, int32_t *active, int32_t *reason);
+
 /* Launch tiling chosen by the plan: out[0..7] = cells per thread along z,
  * threads along z, rows along y, planes along x per CTA, CTAs, kernels per
  * full step, variant (1 register streaming, 2 TMA-staged; plus 10 when the
- * PML slabs run in kernels of their own), ring stages. */
+ * PML slabs run in kernels of their own; 4 one pass per full step, whose
+ * tiling is then reported), ring stages. */
 int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8);
 
 const char *fdtd_status_string(int32_t status);
