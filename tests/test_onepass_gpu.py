@@ -155,7 +155,7 @@ def test_onepass_not_allowed_cases(fd):
     fd.set_backend("gb300.float32")
     g = fd.Grid((16, 16, 16), grid_spacing=155e-9)
     g[0, :, :] = fd.PeriodicBoundary()
-    g[0:3, :, :] = fd.PML()  # a PML after the periodic boundary
+    g[:, 0:3, :] = fd.PML()  # a PML after the periodic boundary
     eng = g._ensure_engine()
     assert eng.step_fusion() == (False, False)
     with pytest.raises(RuntimeError):
