@@ -739,8 +739,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 }
                 return stage;
             };
-            const size_t extra = 2 * (size_t)kl.coef_values * esize + (matE != MAT_FULL ? 16 * (size_t)lut_rows : 0) +
-                                 (matH != MAT_FULL ? 16 * (size_t)lut_rows : 0) + 16 + 128;
+            // material tables: 256 padded rows for an index map, one for a uniform material
+            const size_t extra = 2 * (size_t)kl.coef_values * esize + 4 * esize * (size_t)mat_lut_rows(matE) +
+                                 4 * esize * (size_t)mat_lut_rows(matH) + 16 + 128;
             const long per_sm = 228L * 1024;
             auto smem_of = [&](int TY, size_t stage, int S) {
                 return (size_t)S * stage + (size_t)S * 8 + 2 * onepass_bytes(d->precision, TY, matE, matH, 1) + extra;

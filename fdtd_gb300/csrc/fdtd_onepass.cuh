@@ -126,7 +126,7 @@ __device__ __forceinline__ uint32_t one_psi_row(const GridK &g, unsigned char *s
     return nb;
 }
 
-// Fill the stage of plane p for a role (warp 0, all lanes).
+// Fill the stage of plane p for a role (one warp, all lanes).
 template <class T, int TY, int MATE, int MATH>
 __device__ __forceinline__ void one_fill(const GridK &g, unsigned char *st, uint32_t bar, int p, int role, int k0c,
                                          int j0, const CUtensorMap *tmH, const CUtensorMap *tmE,
@@ -216,7 +216,7 @@ __device__ __forceinline__ void one_E_cells(const GridK &g, const double *__rest
                                             const unsigned char *st, const unsigned char *sp, int i, int j, int k,
                                             int row, int c, typename P::T cour, const typename P::T *lutE,
                                             const typename P::T *ctabE, int k0c, int ob0, int ob1, int sb0, int sb1,
-                                            bool store, typename P::T (&e)[3 * N]) {
+                                            unsigned mask_yz, bool store, typename P::T (&e)[3 * N]) {
     using T = typename P::T;
     using G = OneGeom<T, TY, MATE, MATH>;
     const T *Hn = reinterpret_cast<const T *>(st);
@@ -235,7 +235,7 @@ __device__ __forceinline__ void one_E_cells(const GridK &g, const double *__rest
     for (int q = 0; q < 3 * N; ++q) el[q] = T(0);
     const T kx = Hn[on - 3], ky = Hn[on - 2];  // cell k-1 (the prefix at c = 0)
     const PsiSrc<T> src{st, row, k0c, ctabE};
-    const unsigned slabs = slab_mask_yz(g, j, k, N) | slab_mask_x(g, i);
+    const unsigned slabs = mask_yz | slab_mask_x(g, i);
     thread_E<P, N>(g, wave, i, j, k, cour, hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, src, slabs, store);
 }
 
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(32 * (TY + 1))
     T *ctabE = reinterpret_cast<T *>(smem + (size_t)S * SB + 2 * G::xBytes + 8 * (size_t)S);
     T *ctabH = ctabE + g.coef_values;
     T *lutE = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(ctabH + g.coef_values) + 15) & ~uintptr_t(15));
-    T *lutH = lutE + 4 * (MATE == MAT_FULL ? 0 : g.lut_rows);
+    T *lutH = lutE + 4 * (MATE == MAT_IDS ? 256 : (MATE == MAT_UNIFORM ? 1 : 0));
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int k0c = blockIdx.x * Zc, j0 = blockIdx.y * TY;
@@ -278,6 +278,11 @@ __global__ void __launch_bounds__(32 * (TY + 1))
     // the halo warp's lane l < TY also computes the z-halo cell of row l
     const int hz_row = tz, hz_j = j0 + tz, hz_k = k0c + Zc;
     const bool hz_act = !own && tz < TY && hz_j < ny && hz_k < nz;
+    // slabs along y and z do not change along x: their masks once per thread
+    const unsigned mask_yz = slab_mask_yz(g, j, k0, V);
+    const unsigned hz_mask_yz = slab_mask_yz(g, hz_j, hz_k, 1);
+    // the halo warp, which has no H update, fills the stages
+    const bool filler = !own;
 
     if (tid == 0) {
         abort_flag = 0;
@@ -289,8 +294,10 @@ __global__ void __launch_bounds__(32 * (TY + 1))
         stage_coef_tables<T>(g, ctabE, true);
         stage_coef_tables<T>(g, ctabH, false);
     }
-    if constexpr (MATE != MAT_FULL) stage_material_table<T>(g.mlut_E, g.nlut_E, g.lut_rows, lutE);
-    if constexpr (MATH != MAT_FULL) stage_material_table<T>(g.mlut_H, g.nlut_H, g.lut_rows, lutH);
+    // material tables: 256 padded rows for an index map (every byte reads
+    // inside the table), one row for a uniform material
+    if constexpr (MATE != MAT_FULL) stage_material_table<T>(g.mlut_E, g.nlut_E, MATE == MAT_IDS ? 256 : 1, lutE);
+    if constexpr (MATH != MAT_FULL) stage_material_table<T>(g.mlut_H, g.nlut_H, MATH == MAT_IDS ? 256 : 1, lutH);
     __syncthreads();
     const T *ctE = g.coef_values ? ctabE : nullptr;
     const T *ctH = g.coef_values ? ctabH : nullptr;
@@ -301,7 +308,7 @@ __global__ void __launch_bounds__(32 * (TY + 1))
     };
     int issued = 0;
     for (; issued < min(S, seq.n); ++issued)
-        if (tid < 32) issue(issued);
+        if (filler) issue(issued);
 
     alignas(16) T e[N];
 #pragma unroll
@@ -326,7 +333,8 @@ __global__ void __launch_bounds__(32 * (TY + 1))
                 const bool row_needed = own || role != ONE_EHALO;
                 if (act && row_needed && !(replace && !own)) {
                     one_E_cells<P, V, TY, MATE, MATH>(g, wave, st, r > 0 ? sp : st, p, j, k0, ty, tz * V, c, lutE,
-                                                      ctE, k0c, ob0, ob1, sE0, sE1, own && role == ONE_FULL, e);
+                                                      ctE, k0c, ob0, ob1, sE0, sE1, mask_yz,
+                                                      own && role == ONE_FULL, e);
                 }
                 if (replace && act) ld_vec(e, Xp + ty * G::xPitch + 3 * tz * V);
                 if (act && row_needed) {
@@ -339,7 +347,8 @@ __global__ void __launch_bounds__(32 * (TY + 1))
                         ld_any(e1, Xp + hz_row * G::xPitch + 3 * Zc);
                     } else {
                         one_E_cells<P, 1, TY, MATE, MATH>(g, wave, st, r > 0 ? sp : st, p, hz_j, hz_k, hz_row, Zc,
-                                                          c, lutE, ctE, k0c, ob0, ob1, sE0, sE1, false, e1);
+                                                          c, lutE, ctE, k0c, ob0, ob1, sE0, sE1, hz_mask_yz, false,
+                                                          e1);
                     }
                     st_any(Xc + hz_row * G::xPitch + 3 * Zc, e1);
                 }
@@ -362,14 +371,14 @@ __global__ void __launch_bounds__(32 * (TY + 1))
             const T kx = Xp[ty * G::xPitch + 3 * (tz * V + V)];  // cell k0+V (the z-halo for the last lane)
             const T ky = Xp[ty * G::xPitch + 3 * (tz * V + V) + 1];
             const PsiSrc<T> src{sp, ty, k0c, ctH};
-            const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
+            const unsigned slabs = mask_yz | slab_mask_x(g, i);
             thread_H<P, V, true>(g, wave, i, j, k0, c, ec, e, ej, kx, ky, m, h, hl, sH0, sH1, src, slabs, true);
             st_vec(H + 3 * (((size_t)i * ny + j) * nz + k0), h);
         }
         __syncthreads();
         if (abort_flag) break;
         if (r >= 1 && issued < seq.n) {
-            if (tid < 32) {
+            if (filler) {
                 fence_proxy_async();
                 issue(issued);
             }
