@@ -636,7 +636,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // Allowed for float32 plans whose every PML slab precedes any periodic
     // boundary, with periodic boundaries only along x, no object or source on
     // a periodic plane and no feedback source; used when the caller gave the
-    // second buffers and asked for it (or automatically from 8M cells).
+    // second buffers and asked for it.
     if (d->step_fusion < 0 || d->step_fusion > 2) return FDTD_ERR_ARGUMENT;
     p.onepass = p.onepass_ok = p.onepass_hcopy = p.onepass_why = 0;
     GridK kl;  // tiling and stage layout of the one-pass kernel
@@ -675,7 +675,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 (!d->psi_alt[b][0] || !d->psi_alt[b][1] || !aligned16(d->psi_alt[b][0]) ||
                  !aligned16(d->psi_alt[b][1])))
                 alt = false;
-        const bool want = d->step_fusion == 2 || (d->step_fusion == 0 && ncell >= (8L << 20));
+        // automatic choice: never -- the two-pass plans measured faster on every
+        // configuration (the one-pass stage holds about twice the bytes per cell,
+        // so fewer planes are in flight per SM and the pass is latency-bound)
+        const bool want = d->step_fusion == 2;
         if (ok && !alt) refuse(7);
         p.onepass_why = why;
         if (want && ok && alt) {

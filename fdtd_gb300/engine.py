@@ -303,7 +303,7 @@ class Engine:
         materials (0 a one-byte index into a table of distinct value triples,
         or nothing for a uniform material, where the materials allow; 1 the
         full arrays), and whether full steps run as one pass each (0 auto:
-        float32 grids of 8M cells or more that allow it; 1 never; 2 always
+        currently never, the two-pass plans measured faster; 1 never; 2
         where the grid allows it, else RuntimeError); 0 keeps the automatic
         choice.  The one-pass step uses tile_rows 4 or 8, stages >= 3 and
         x_chunk when given."""
@@ -513,7 +513,8 @@ class Engine:
 
         # one pass per step: the library decides whether the grid allows it;
         # the second buffers it needs are allocated only when it will be used
-        # (float32 grids of 8M cells or more, or when asked)
+        # (when asked: the automatic choice keeps the two-pass plans, which
+        # measured faster on every benchmark grid)
         req = self.tuning["step_fusion"]
         if self._alt is not None and (req == 1 or not self._alt_fits()):
             self._alt = None
@@ -527,8 +528,7 @@ class Engine:
         allowed, active, why = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
         _native.check(lib.fdtd_plan_step_fusion(plan, ctypes.byref(allowed), ctypes.byref(active), ctypes.byref(why)),
                       "fdtd_plan_step_fusion")
-        ncell = g.Nx * g.Ny * g.Nz
-        want = req == 2 or (req == 0 and g.precision == "float32" and ncell >= (8 << 20))
+        want = req == 2
         if allowed.value and want and not active.value and self._alt is None:
             try:
                 self._alloc_alt()

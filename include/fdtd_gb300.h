@@ -196,9 +196,9 @@ typedef struct {
      * fdtd_run_capture use the two-pass kernels.  Float32 plans whose PML
      * slabs all precede any periodic boundary, with periodic boundaries only
      * along x, no object or source on a periodic plane, and without a
-     * feedback source.  step_fusion: 0 automatic (float32 grids of 8M cells
-     * or more when the buffers are given), 1 off, 2 on where the grid allows
-     * it.  fdtd_plan_step_fusion reports whether a grid allows it (before any
+     * feedback source.  step_fusion: 0 automatic (currently off: the
+     * two-pass plans measured faster on every benchmark grid), 1 off, 2 on
+     * where the grid allows it.  fdtd_plan_step_fusion reports whether a grid allows it (before any
      * buffer is allocated), whether the plan uses it, and why not. */
     int32_t step_fusion;
     int32_t reserved_fusion;
