@@ -94,6 +94,11 @@ def parse():
                    help="config 3: steps of the long-run float32 / float32c trace error against float64 (0 = off)")
     p.add_argument("--skip-configs", action="store_true",
                    help="skip configs 2 and 5 (forward throughput, roofline and long-run errors)")
+    p.add_argument("--step-fusion", type=int, default=0,
+                   help="0 auto, 1 two passes per step, 2 one pass per step (float32 grids that allow it)")
+    p.add_argument("--forward-only", choices=["c2", "c5"], default=None,
+                   help="only --warmup + --steps float32 forward steps of the named config (a profiling target; "
+                        "prints its own JSON line)")
     p.add_argument("--configs-only", action="store_true",
                    help="only configs 2 and 5 (prints its own JSON line)")
     return p.parse_args()
@@ -232,7 +237,7 @@ def build_grid(fd, scenes, prec, n, eps, args):
     g = scenes.c3(fd, n=n, pml=pml, eps=eps, detector=True)
     eng = g._ensure_engine()
     eng.set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages, x_chunk=args.x_chunk,
-                   pml_mode=args.pml_mode, materials=args.materials)
+                   pml_mode=args.pml_mode, materials=args.materials, step_fusion=args.step_fusion)
     return g, eng
 
 
@@ -767,6 +772,24 @@ def main():
         reference_arm(args)
     elif args.impl == "reference-gpu":
         reference_gpu_arm(args)
+    elif args.forward_only:
+        import torch
+
+        import fdtd_gb300 as fd
+        from fdtd_gb300 import scenes
+
+        fd.set_backend("gb300.float32")
+        g = scenes.c2(fd) if args.forward_only == "c2" else scenes.c5(fd)
+        g.run(args.warmup, progress_bar=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.run(args.steps, progress_bar=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / max(1, args.steps)
+        print(json.dumps({"forward": args.forward_only, "ms_per_step": ms,
+                          "gcells": g.Nx * g.Ny * g.Nz / ms / 1e6, "tiling": g._engine.tiling()}), flush=True)
     elif args.configs_only:
         import fdtd_gb300 as fd
         from fdtd_gb300 import scenes
