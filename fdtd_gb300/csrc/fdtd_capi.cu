@@ -632,6 +632,48 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     build_csr(t, items, srcE0, d->n_sources_E, se_off, se_idx);
     build_csr(t, items, srcH0, d->n_sources_H, sh_off, sh_idx);
 
+    // Launch order of the staged passes: the tiles that carry more work per
+    // plane (object cells, weighted by the coefficient values they read, and
+    // cells of the PML slabs inside the fused pass) first, so that they run
+    // in the first waves instead of finishing last; the rest in grid order.
+    std::vector<int> cta_order;
+    if (p.variant == 2) {
+        const long ncta = (long)t.gz * t.gy * t.gx;
+        const int zc = t.V * t.TZ;
+        std::vector<double> extra(ncta, 0.0);
+        auto add_box = [&](const int32_t lo[3], const int32_t hi[3], double w) {
+            int r[6];
+            cta_range(t, lo, hi, r);
+            for (int cx = r[4]; cx <= r[5]; ++cx)
+                for (int cy = r[2]; cy <= r[3]; ++cy)
+                    for (int cz = r[0]; cz <= r[1]; ++cz) {
+                        const long ox = std::min(hi[0], (cx + 1) * t.XC) - std::max(lo[0], cx * t.XC);
+                        const long oy = std::min(hi[1], (cy + 1) * t.TY) - std::max(lo[1], cy * t.TY);
+                        const long oz = std::min(hi[2], (cz + 1) * zc) - std::max(lo[2], cz * zc);
+                        if (ox > 0 && oy > 0 && oz > 0) extra[cz + t.gz * (cy + (long)t.gy * cx)] += w * ox * oy * oz;
+                    }
+        };
+        for (int q = 0; q < srcE0; ++q) {
+            const ItemK &o = items[q];
+            add_box(o.lo, o.hi, o.kind == FDTD_ITEM_ANISOTROPIC ? 3.0 : (o.kind == FDTD_ITEM_ABSORBING ? 2.0 : 1.0));
+        }
+        const int fused = p.pml_split ? p.fused_slabs : g.nslab;
+        for (int sl = 0; sl < fused; ++sl) {
+            const SlabK &S = g.slab[sl];
+            int32_t lo[3] = {0, 0, 0}, hi[3] = {d->nx, d->ny, d->nz};
+            lo[S.axis] = S.start;
+            hi[S.axis] = S.start + S.th;
+            add_box(lo, hi, 1.0);
+        }
+        bool any = false;
+        for (double w : extra) any |= w > 0.0;
+        if (any) {
+            cta_order.resize(ncta);
+            for (long c = 0; c < ncta; ++c) cta_order[c] = (int)c;
+            std::stable_sort(cta_order.begin(), cta_order.end(), [&](int a, int b) { return extra[a] > extra[b]; });
+        }
+    }
+
     // ---- one pass per time step (fdtd_onepass.cuh) ----
     // Allowed for float32 plans whose every PML slab precedes any periodic
     // boundary, with periodic boundaries only along x, no object or source on
@@ -837,7 +879,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     const size_t b_lists = align(sizeof(int) * (obj_off.size() + obj_idx.size() + se_off.size() + se_idx.size() +
                                                 sh_off.size() + sh_idx.size() + oo_off.size() + oo_idx.size() +
                                                 ose_off.size() + ose_idx.size() + osh_off.size() + osh_idx.size() +
-                                                12));
+                                                cta_order.size() + 13));
     const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
     const size_t b_status = 256;
     std::vector<char> host(b_items + b_lists + b_runs + b_status, 0);
@@ -863,6 +905,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     put(ose_idx, at_ose_idx);
     put(osh_off, at_osh_off);
     put(osh_idx, at_osh_idx);
+    size_t at_order;
+    put(cta_order, at_order);
     if (!runs.empty()) memcpy(host.data() + b_items + b_lists, runs.data(), sizeof(int2) * runs.size());
     ce = cudaMalloc(&p.dev_mem, host.size());
     if (ce != cudaSuccess) return cuda_fail(ce);
@@ -881,6 +925,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.srcE_idx = dl + at_se_idx;
     g.srcH_off = dl + at_sh_off;
     g.srcH_idx = dl + at_sh_idx;
+    g.cta_order = cta_order.empty() ? nullptr : dl + at_order;
     p.runs = (const int2 *)(base + b_items + b_lists);
     g.status = (int *)(base + b_items + b_lists + b_runs);
     if (p.variant == 2) {
@@ -933,6 +978,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             k.srcH_off = dl + at_osh_off;
             k.srcH_idx = dl + at_osh_idx;
             k.fuse_src_E = k.fuse_src_H = 1;
+            k.cta_order = nullptr;  // the one-pass kernel launches in grid order
             void *Ea = d->E, *Ha = d->H, *Eb = d->E_alt, *Hb = d->H_alt;
             k.E = dir == 0 ? Eb : Ea;  // written
             k.H = dir == 0 ? Hb : Ha;

@@ -84,6 +84,14 @@ __device__ __forceinline__ void apply_object_cell(const ItemK &o, size_t li, typ
 
 __device__ __forceinline__ bool aligned16_ptr(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
+// Ask L2 for the `bytes` bytes at p (one request per 128-byte line): the
+// object coefficients of the next plane, so that its loads hit L2 instead of
+// waiting for DRAM inside the plane loop.
+__device__ __forceinline__ void prefetch_l2(const void *p, int bytes) {
+    const char *c = reinterpret_cast<const char *>(p);
+    for (int o = 0; o < bytes; o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + o));
+}
+
 // Objects of a thread's V cells (fdtd/objects.py:92-129, 198-221, 256-269),
 // items in list order; each cell gets the same operations in the same order
 // as one at a time.  In float32, where all V cells lie in a box and their
@@ -106,11 +114,15 @@ __device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, in
         if constexpr (V > 1 && sizeof(T) == 4) {
             const size_t li = k0 >= o.lo[2] ? box_index(o, i, j, k0) : 0;
             const bool whole = k0 >= o.lo[2] && k0 + V <= o.hi[2];
+            // the next plane of the box one plane ahead
+            const size_t plane = (size_t)o.bny * o.bnz;
+            const bool ahead = i + 1 < o.hi[0];
             if (whole && o.kind == FDTD_ITEM_ANISOTROPIC) {
                 const T *src = (const T *)o.coef[0] + 9 * li;
                 if (aligned16_ptr(src)) {
                     alignas(16) T M[9 * V];
                     ld_vec_ro(M, src);
+                    if (ahead) prefetch_l2(src + 9 * plane, 9 * V * (int)sizeof(T));
 #pragma unroll
                     for (int v = 0; v < V; ++v) {
                         const T *m = M + 9 * v;
@@ -127,6 +139,7 @@ __device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, in
                 if (aligned16_ptr(src)) {
                     alignas(16) T cf[3 * V];
                     ld_vec_ro(cf, src);
+                    if (ahead) prefetch_l2(src + 3 * plane, 3 * V * (int)sizeof(T));
 #pragma unroll
                     for (int v = 0; v < V; ++v)
 #pragma unroll
@@ -140,6 +153,10 @@ __device__ __forceinline__ void apply_objects_v(const GridK &g, int i, int j, in
                     alignas(16) T r[3 * V], ci[3 * V];
                     ld_vec_ro(r, rs);
                     ld_vec_ro(ci, cs);
+                    if (ahead) {
+                        prefetch_l2(rs + 3 * plane, 3 * V * (int)sizeof(T));
+                        prefetch_l2(cs + 3 * plane, 3 * V * (int)sizeof(T));
+                    }
                     if constexpr (sizeof(T) == 4) {
 #pragma unroll
                         for (int q = 0; q < 3 * V; ++q) {

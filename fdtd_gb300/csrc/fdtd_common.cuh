@@ -81,6 +81,7 @@ struct GridK {
     int lut_rows;  // padded 4-value rows reserved for the table in shared memory
     const unsigned char *mid_E, *mid_H;  // one-byte material indices (MAT_IDS)
     int periodic_x;  // one-pass step: a periodic boundary along x follows the PML slabs
+    const int *cta_order;  // staged passes: tile of each launched block, heaviest first (null: grid order)
 };
 
 template <class T>

@@ -82,6 +82,24 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
+// The tile a CTA works on: blocks are launched in the order of g.cta_order
+// when the plan has one (the tiles that carry objects or PML slabs first, so
+// that they do not finish last), else in grid order.
+struct TileId {
+    int bx, by, bz, cta;
+};
+
+__device__ __forceinline__ TileId tile_of(const GridK &g) {
+    int lin = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if (g.cta_order) lin = g.cta_order[lin];
+    TileId t;
+    t.cta = lin;
+    t.bx = lin % gridDim.x;
+    t.by = (lin / gridDim.x) % gridDim.y;
+    t.bz = lin / (gridDim.x * gridDim.y);
+    return t;
+}
+
 // Byte layout of the field part of one stage: the neighbour tile (TY+1 rows
 // of 3*Zc+4 values), the own field tile (TY rows of 3*Zc values), the own
 // material tile (values, indices or nothing) and, compensated, the own
@@ -256,12 +274,13 @@ __global__ void __launch_bounds__(TZ *TY)
     T *mlut = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(ctab + g.coef_values) + 15) & ~uintptr_t(15));
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
+    const TileId tile = tile_of(g);
+    const int k0c = tile.bx * G::Zc, j0 = tile.by * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
-    const int xa = blockIdx.z * g.XC, xb = min(nx, xa + g.XC);
+    const int xa = tile.bz * g.XC, xb = min(nx, xa + g.XC);
     const int np = xb - xa;
     const bool act = (j < ny) && (k0 < nz);
-    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int cta = tile.cta;
     const T c = courant_of<T>(g);
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
@@ -372,13 +391,14 @@ __global__ void __launch_bounds__(TZ *TY)
     T *mlut = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(ctab + g.coef_values) + 15) & ~uintptr_t(15));
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0c = blockIdx.x * G::Zc, j0 = blockIdx.y * TY;
+    const TileId tile = tile_of(g);
+    const int k0c = tile.bx * G::Zc, j0 = tile.by * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
-    const int xa = blockIdx.z * g.XC, xb = min(nx, xa + g.XC);
+    const int xa = tile.bz * g.XC, xb = min(nx, xa + g.XC);
     const int np = xb - xa;
     const int nfill = np + 1;  // E of plane xb is needed by the last plane
     const bool act = (j < ny) && (k0 < nz);
-    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int cta = tile.cta;
     const T c = courant_of<T>(g);
     T *H = (T *)g.H;
     T *Hlo = (T *)g.Hlo;
