@@ -322,6 +322,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     Tiling t{};
     int ctas_per_sm = 2;
     bool use_tma = tma;
+    // staged passes: ring depth, stage bytes and auxiliary slot offsets of the E (0) and H (1) pass
+    int pass_stages[2] = {0, 0}, pass_stage_bytes[2] = {0, 0};
+    int pass_psi_off[2][kMaxSlabs] = {{0}};
     if (use_tma) {
         t.V = vmax;
         if (d->tile_rows != 0 && d->tile_rows != 4 && d->tile_rows != 8 && d->tile_rows != 16)
@@ -332,9 +335,11 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         // (rows copied per stage); returns the stage bytes and fills the slot
         // offsets and pitches of the plan
         const int lut_rows = std::max(mat_lut_rows(mat_want[0]), mat_lut_rows(mat_want[1]));
-        auto stage_layout = [&](int TY, int TZ) -> size_t {
+        auto stage_layout = [&](int TY, int TZ, int m0 = -1, int *off_out = nullptr) -> size_t {
             const int Zc = TZ * t.V;
-            const size_t field = tma_stage_bytes(d->precision, TY, mat_want[0], mat_want[1]);
+            // field part: the larger of the two passes', or one pass's (m0: its material mode)
+            const size_t field = m0 < 0 ? tma_stage_bytes(d->precision, TY, mat_want[0], mat_want[1])
+                                        : tma_stage_bytes(d->precision, TY, m0, m0);
             struct Slot {
                 int axis;
                 size_t bytes;
@@ -371,7 +376,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 sl.off = stage;
                 stage += (sl.bytes + 127) & ~(size_t)127;
             }
-            for (int s = 0; s < ks; ++s) g.psi_off[s] = (int)slots[slot_of[s]].off;
+            for (int s = 0; s < ks; ++s) (off_out ? off_out : g.psi_off)[s] = (int)slots[slot_of[s]].off;
             return stage;
         };
         int coef = 0;
@@ -435,6 +440,24 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             g.stages = S;
             ctas_per_sm = resident(smem);
             p.variant = 2;
+            // each pass lays out its own stages inside the same shared memory:
+            // a pass whose stage is smaller than the larger one gets a deeper
+            // ring (the H pass holds two planes at once, so its loads in flight
+            // are one stage fewer; config 2 with full permittivity runs its H
+            // pass on 4-row tiles sized for the E pass's material tile)
+            for (int pass = 0; pass < 2; ++pass) {
+                const size_t sb = stage_layout(t.TY, t.TZ, mat_want[pass], pass_psi_off[pass]);
+                int sp = S;
+                if (d->stages == 0)
+                    for (int q = 8; q > S; --q)
+                        if (smem_of(sb, q) <= smem) {
+                            sp = q;
+                            break;
+                        }
+                pass_stage_bytes[pass] = (int)sb;
+                pass_stages[pass] = sp;
+            }
+            stage_layout(t.TY, t.TZ);  // g.psi_off of the shared layout again
             g.mat_E = mat_want[0];
             g.mat_H = mat_want[1];
             g.mlut_E = d->eps_table;
@@ -939,6 +962,15 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     if (p.pml_split) {
         p.kf.nslab = p.fused_slabs;
         p.kf.nslab_fused = p.fused_slabs;
+    }
+    p.kfH = p.kf;
+    if (p.variant == 2) {
+        GridK *pass_k[2] = {&p.kf, &p.kfH};
+        for (int pass = 0; pass < 2; ++pass) {
+            pass_k[pass]->stages = pass_stages[pass];
+            pass_k[pass]->stage_bytes = pass_stage_bytes[pass];
+            for (int s = 0; s < kMaxSlabs; ++s) pass_k[pass]->psi_off[s] = pass_psi_off[pass][s];
+        }
     }
 
     if (p.onepass) {

@@ -52,7 +52,7 @@ static void launch_tma_mat(Plan &p, bool is_E, const double *wave, cudaStream_t 
             p.kf, wave, m[MAP_H_NBR], m[MAP_E_OWN], m[MAP_IE], m[P::COMP ? MAP_ELO : MAP_E_OWN]);
     else
         k_update_H_tma<P, TZ, TY, MAT><<<p.grid, block, p.smem_bytes, st>>>(
-            p.kf, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
+            p.kfH, wave, m[MAP_E_NBR], m[MAP_H_OWN], m[MAP_MU], m[P::COMP ? MAP_HLO : MAP_H_OWN]);
 }
 
 template <class P, int TZ, int TY>

@@ -29,6 +29,7 @@ struct Plan {
     int precision;
     GridK k;           // the grid with every PML slab (epilogue and adjoint kernels)
     GridK kf;          // what the fused pass sees: k, or k without slabs when they run on their own
+    GridK kfH;         // the same for the H pass of staged plans (its own ring depth and stage layout)
     int pml_split;     // 1: PML slabs from fused_slabs on run as EPI_PML kernels after the fused pass
     int fused_slabs;   // with pml_split: leading slabs (normal to x or y) kept in the fused pass
     int V;             // cells per thread along z
