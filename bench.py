@@ -780,6 +780,9 @@ def main():
 
         fd.set_backend("gb300.float32")
         g = scenes.c2(fd) if args.forward_only == "c2" else scenes.c5(fd)
+        g._ensure_engine().set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages,
+                                      x_chunk=args.x_chunk, pml_mode=args.pml_mode, materials=args.materials,
+                                      step_fusion=args.step_fusion)
         g.run(args.warmup, progress_bar=False)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
