@@ -489,13 +489,15 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         // Staged kernels: about twenty waves of the resident CTAs, so the
         // partly filled last wave costs little (measured on 768^3 with one CTA
         // per SM: 3.8 waves 58.7, 7.6 waves 61.4, 22.7 waves 63.1 Gcell/s),
-        // with at least 32 planes per chunk (a chunk refills the ring and
-        // re-reads one halo plane).  Register kernels: register_chunk.
+        // with at least 12 planes per chunk (a chunk refills the ring and
+        // re-reads one halo plane; configs 2 and 5, which reach only three
+        // waves with 32-plane chunks, measured best at 12).  Register
+        // kernels: register_chunk.
         const long cols = (long)t.gz * t.gy;
         const long wave = (long)n_sm * ctas_per_sm;
         if (use_tma) {
             long chunks = cols >= 20L * wave ? 1 : (20L * wave + cols - 1) / cols;
-            chunks = std::max(1L, std::min(chunks, std::max(1L, (long)d->nx / 32)));
+            chunks = std::max(1L, std::min(chunks, std::max(1L, (long)d->nx / 12)));
             t.XC = (int)((d->nx + chunks - 1) / chunks);
         } else {
             t.XC = register_chunk(d->nx, cols, wave);
