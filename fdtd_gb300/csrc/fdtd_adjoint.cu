@@ -1,9 +1,90 @@
 // Launch sequence of the reverse-time adjoint (fdtd_adjoint_run), float32 and
 // float64 instantiations.
 #include "fdtd_adjoint.cuh"
+#include "fdtd_adjoint_tma.cuh"
+#include "fdtd_launch.cuh"
 #include "fdtd_plan.hpp"
 
 namespace fdtd {
+
+// ---- TMA-staged transposed passes (fdtd_adjoint_tma.cuh) -------------------
+// Used by plans whose forward passes are TMA-staged with the PML slabs in
+// kernels of their own; they reuse the forward tiling, launch order and
+// material copies.  Tensor maps of the adjoint fields are encoded per call
+// (the caller's buffers), those of the materials' neighbour footprints too
+// (a few host calls per fdtd_adjoint_run).
+
+static int optin_smem() {
+    static int v = 0;
+    if (v == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    return v;
+}
+
+template <class T, int TZ, int TY, int MAT>
+static int adj_staged_launch(const Plan &p, const GridK &g0, bool is_H, cudaStream_t st) {
+    using G = AdjGeom<T, TZ, TY, MAT>;
+    const int esz = (int)sizeof(T);
+    GridK g = g0;
+    g.stage_bytes = G::stageBytes;
+    // ring depth: two CTAs per SM with at least three stages where that fits
+    const size_t extra = 16 + 4 * 256 * (size_t)esz + 128;
+    auto smem_of = [&](int S) { return (size_t)S * (G::stageBytes + 8) + extra; };
+    int S = 0;
+    for (int q = 6; q >= 3 && S == 0; --q)
+        if ((long)smem_of(q) + 1024 <= 114L * 1024 && smem_of(q) <= (size_t)optin_smem()) S = q;
+    for (int q = 6; q >= 2 && S == 0; --q)
+        if (smem_of(q) <= (size_t)optin_smem()) S = q;
+    if (S == 0) return FDTD_ERR_UNSUPPORTED;
+    g.stages = S;
+    const size_t smem = smem_of(S);
+    // neighbour tile of the field read, its material footprint, own tile of the field updated
+    CUtensorMap mN, mM, mO;
+    const void *read = is_H ? g.H : g.E, *upd = is_H ? g.E : g.H;
+    bool ok = encode_field_map(&mN, read, g, esz, G::boxN, TY + 1) && encode_field_map(&mO, upd, g, esz, G::boxO, TY);
+    const int mat = is_H ? g.mat_H : g.mat_E;
+    if (mat == MAT_FULL) ok = ok && encode_field_map(&mM, is_H ? g.imu : g.ie, g, esz, G::boxN, TY + 1);
+    else if (mat == MAT_IDS) ok = ok && encode_index_map(&mM, is_H ? p.index_H : p.index_E, g, G::idxN, TY + 1);
+    else mM = mN;
+    if (!ok) return FDTD_ERR_UNSUPPORTED;
+    const dim3 block(TZ, TY, 1);
+    cudaError_t e;
+    if (is_H) {
+        e = cudaFuncSetAttribute(k_adj_H_tma<T, TZ, TY, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_adj_H_tma<T, TZ, TY, MAT><<<p.grid, block, smem, st>>>(g, mN, mM, mO);
+    } else {
+        e = cudaFuncSetAttribute(k_adj_E_tma<T, TZ, TY, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_adj_E_tma<T, TZ, TY, MAT><<<p.grid, block, smem, st>>>(g, mN, mM, mO);
+    }
+    if (e != cudaSuccess) {
+        set_last_cuda_error((int)e);
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+template <class T, int TZ, int TY>
+static int adj_staged_mat(const Plan &p, const GridK &g, bool is_H, cudaStream_t st) {
+    switch (is_H ? g.mat_H : g.mat_E) {
+        case MAT_IDS:
+            return adj_staged_launch<T, TZ, TY, MAT_IDS>(p, g, is_H, st);
+        case MAT_UNIFORM:
+            return adj_staged_launch<T, TZ, TY, MAT_UNIFORM>(p, g, is_H, st);
+        default:
+            return adj_staged_launch<T, TZ, TY, MAT_FULL>(p, g, is_H, st);
+    }
+}
+
+// One transposed bulk pass of a staged plan (the forward passes' tile shape).
+template <class T>
+static int adj_staged(const Plan &p, const GridK &g, bool is_H, cudaStream_t st) {
+    if (p.k.TY == 16) return adj_staged_mat<T, 16, 16>(p, g, is_H, st);
+    if (p.k.TY == 8) return adj_staged_mat<T, 32, 8>(p, g, is_H, st);
+    return adj_staged_mat<T, 32, 4>(p, g, is_H, st);
+}
 
 static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
 
@@ -76,6 +157,13 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
     // for the transposes: slab-free bulk passes, then one kernel per slab
     GridK gb = g;
     if (p.pml_split) gb.nslab = 0;
+    // staged forward plans with the slabs on their own: staged transposed passes
+    const bool staged = p.variant == 2 && p.pml_split && p.adj_V == (sizeof(T) == 4 ? 4 : 2);
+    GridK gs = p.k;  // the forward staged tiling, launch order and material copies
+    gs.E = a->lam_E;
+    gs.H = a->lam_H;
+    gs.Elo = gs.Hlo = nullptr;
+    gs.nslab = 0;
     auto slab_cells = [&](const SlabK &S) {
         return (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) * (S.axis == 2 ? S.th : g.nz);
     };
@@ -114,7 +202,12 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
                     g, op.slab, (T *)a->aux_H[p.slab_boundary[op.slab]][par]);
             }
         }
-        k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
+        if (staged) {
+            const int rc = adj_staged<T>(p, gs, true, st);
+            if (rc != FDTD_OK) return rc;
+        } else {
+            k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
+        }
         if (p.pml_split)
             for (int q = 0; q < g.nslab; ++q)
                 launch_adj_slab<T, false>(g, x, q, slab_cells(g.slab[q]), st);
@@ -149,7 +242,12 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
                     g, op.slab, (T *)a->aux_E[p.slab_boundary[op.slab]][par]);
             }
         }
-        k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
+        if (staged) {
+            const int rc = adj_staged<T>(p, gs, false, st);
+            if (rc != FDTD_OK) return rc;
+        } else {
+            k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
+        }
         if (p.pml_split)
             for (int q = 0; q < g.nslab; ++q)
                 launch_adj_slab<T, true>(g, x, q, slab_cells(g.slab[q]), st);

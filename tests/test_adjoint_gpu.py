@@ -40,12 +40,12 @@ def native():
     return _native.load()
 
 
-def gb_loss_and_grad(fd, sc, design_values, precision, checkpoint_every, pml_mode=0):
+def gb_loss_and_grad(fd, sc, design_values, precision, checkpoint_every, pml_mode=0, variant=0):
     fd.set_backend("gb300." + precision)
     grid, obj = sc.build(fd)
     sc.detectors(fd, grid)
-    if pml_mode:
-        grid._ensure_engine().set_tuning(pml_mode=pml_mode)
+    if pml_mode or variant:
+        grid._ensure_engine().set_tuning(pml_mode=pml_mode, variant=variant)
     p = torch.tensor(np.asarray(design_values), dtype=torch.float64, device="cuda", requires_grad=True)
     outs = fd.adjoint.run(grid, sc.steps, design={obj: p}, checkpoint_every=checkpoint_every)
     loss = sc.gb_loss(outs, torch)
@@ -141,6 +141,30 @@ class MixedScene:
         e = outs["block"]["E"].to(torch.float64)
         h = outs["block"]["H"].to(torch.float64)
         return (e ** 2).sum() + 0.5 * (h[..., 1] * h[..., 2]).sum()
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+@pytest.mark.parametrize("name", sorted(adjoint_scenes.SCENES))
+def test_staged_adjoint_matches_reference_autograd(fd, name, precision):
+    """TMA-staged forward passes with the PML slabs in kernels of their own
+    (the plan of large grids) run TMA-staged transposed passes: against the
+    reference's autograd, and bit for bit against the register-streaming
+    transposed passes of the same split plan."""
+    ref = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    sc = adjoint_scenes.SCENES[name]
+    loss, grad, grid = gb_loss_and_grad(fd, sc, ref["design"], precision, checkpoint_every=9, pml_mode=2,
+                                        variant=2)
+    info = grid._engine.tiling()
+    assert info["variant"] == 2 and info["pml_split"] == 1, info
+    grid._engine.check_status()
+    tol = TOL64 if precision == "float64" else TOL32
+    assert abs(loss - float(ref["loss"])) <= tol * abs(float(ref["loss"]))
+    err = rel_l2(grad, ref["grad"])
+    assert err <= tol, f"{name} {precision}: gradient relative L2 {err:.3e}"
+    loss_r, grad_r, grid_r = gb_loss_and_grad(fd, sc, ref["design"], precision, checkpoint_every=9, pml_mode=2,
+                                              variant=1)
+    assert grid_r._engine.tiling()["variant"] == 1
+    assert loss_r == loss and np.array_equal(grad_r, grad), f"max |diff| {np.abs(grad_r - grad).max():.3e}"
 
 
 @pytest.mark.parametrize("pml_mode", [0, 2])
