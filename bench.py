@@ -495,6 +495,27 @@ def adjoint_ratio(fd, scenes, which, fd_check=True):
                     "adjoint_ms": t_adj * 1e3, "adjoint_over_forward": t_adj / t_fwd,
                     "precision": "f32 fields, f64 gradient accumulation",
                     "loss": float(loss.detach()), "grad_norm": float(p.grad.norm())}
+        grad_ck = p.grad.detach().clone()
+        del g, p, outs, loss
+        gc.collect()
+        torch.cuda.empty_cache()
+        # the same run keeping the design-box curls of every step in device
+        # memory (checkpoint_every=None: one segment, no recompute)
+        g = make()
+        p = design()
+        sync()
+        t = time.perf_counter()
+        outs = fd.adjoint.run(g, steps, {g.design: p}, checkpoint_every=None)
+        loss = loss_of(outs)
+        loss.backward()
+        sync()
+        t_st = time.perf_counter() - t
+        cells = g.design.Nx * g.design.Ny * g.design.Nz
+        out[cfg]["all_curls_kept"] = {
+            "adjoint_ms": t_st * 1e3, "adjoint_over_forward": t_st / t_fwd,
+            "curl_store_gb": steps * cells * 3 * 4 / 1e9,
+            "grad_rel_diff_vs_checkpointed": float((p.grad - grad_ck).norm() / grad_ck.norm())}
+        del grad_ck
         if cfg == "c4" and fd_check:
             out[cfg]["fd_check"] = c4_finite_differences(fd, scenes, p.grad.detach().cpu().numpy(), loss_of)
         del g, p, outs, loss
