@@ -80,7 +80,7 @@ class GridDesc(ctypes.Structure):
         ("grid_spacing", ctypes.c_double), ("materials_scaled", c_int32),
         ("eps_table", c_void_p), ("n_eps_table", c_int32), ("eps_index", c_void_p),
         ("mu_table", c_void_p), ("n_mu_table", c_int32), ("mu_index", c_void_p),
-        ("step_fusion", c_int32), ("reserved_fusion", c_int32),
+        ("step_fusion", c_int32), ("persistent", c_int32),
         ("E_alt", c_void_p), ("H_alt", c_void_p),
         ("psi_alt", (c_void_p * 2) * MAX_BOUNDARIES),
     ]

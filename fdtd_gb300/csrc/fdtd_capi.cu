@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "fdtd_kernels.cuh"
+#include "fdtd_persistent.cuh"
 #include "fdtd_plan.hpp"
 
 struct fdtd_plan {
@@ -906,7 +907,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                                                 ose_off.size() + ose_idx.size() + osh_off.size() + osh_idx.size() +
                                                 cta_order.size() + 13));
     const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
-    const size_t b_status = 256;
+    const size_t b_status = 512;  // status word, then the persistent loop's barrier counter
     std::vector<char> host(b_items + b_lists + b_runs + b_status, 0);
     if (nitems) memcpy(host.data(), items.data(), sizeof(ItemK) * nitems);
     int *lists = (int *)(host.data() + b_items);
@@ -953,6 +954,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.cta_order = cta_order.empty() ? nullptr : dl + at_order;
     p.runs = (const int2 *)(base + b_items + b_lists);
     g.status = (int *)(base + b_items + b_lists + b_runs);
+    p.persist_bar = (unsigned *)(base + b_items + b_lists + b_runs + 256);
     if (p.variant == 2) {
         const int rc = d->precision == FDTD_FLOAT32    ? prepare_tma_f32(p)
                        : d->precision == FDTD_FLOAT32C ? prepare_tma_f32c(p)
@@ -1035,6 +1037,17 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         }
     }
 
+    // persistent time loop (fdtd_persistent.cuh): small register-streaming
+    // plans with nothing between the half steps but gathers and DFT sums
+    if (d->persistent < 0 || d->persistent > 2) return FDTD_ERR_ARGUMENT;
+    {
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        p.persist_ok = coop && p.variant == 1 && p.epi_E.empty() && p.epi_H.empty() && !p.has_feedback &&
+                       p.n_current == 0 && (int)p.dft.size() <= kPersistMaxDft;
+        p.persistent = p.persist_ok && (d->persistent == 2 || (d->persistent == 0 && ncell < (8L << 20)));
+        p.persist_blocks = 0;
+    }
     p.stats_ctas = std::max(1, std::min(4 * n_sm, FDTD_STATS_STATIC_MAX_ROWS));
     p.device = dev;
     p.launches_per_step = 2 + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
@@ -1336,8 +1349,8 @@ int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8) {
     out8[2] = p.k.TY;
     out8[3] = p.k.XC;
     out8[4] = (int64_t)p.grid.x * p.grid.y * p.grid.z;
-    out8[5] = p.launches_per_step;
-    out8[6] = p.variant + (p.pml_split ? 10 : 0);
+    out8[5] = p.persistent ? 1 : p.launches_per_step;  // persistent: one launch per fdtd_run call
+    out8[6] = p.persistent ? 5 : p.variant + (p.pml_split ? 10 : 0);
     out8[7] = p.k.stages;
     return FDTD_OK;
 }

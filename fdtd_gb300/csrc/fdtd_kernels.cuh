@@ -21,18 +21,20 @@ namespace fdtd {
 // Register-streaming kernels: neighbour values come from global memory
 // (L1/L2) and from the lane to the left/right; used for shapes the staged
 // kernels do not take (nz not a multiple of the vector width, unaligned data).
+// One tile of the E half (bx, by, bz: tile coordinates; cta: its index in the
+// per-CTA lists), for the one-tile-per-block kernel and the persistent one.
 template <class P, int V>
-__global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const double *__restrict__ wave) {
+__device__ __forceinline__ void tile_update_E(const GridK &g, const double *__restrict__ wave, int bx, int by, int bz,
+                                              int cta) {
     using T = typename P::T;
     constexpr int N = 3 * V;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0 = (blockIdx.x * g.TZ + tz) * V;
-    const int j = blockIdx.y * g.TY + ty;
-    const int xa = blockIdx.z * g.XC;
+    const int k0 = (bx * g.TZ + tz) * V;
+    const int j = by * g.TY + ty;
+    const int xa = bz * g.XC;
     const int xb = min(nx, xa + g.XC);
     const bool act = (j < ny) && (k0 < nz);
-    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     const T c = courant_of<T>(g);
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
@@ -89,17 +91,23 @@ __global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const doub
 }
 
 template <class P, int V>
-__global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const double *__restrict__ wave) {
+__global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const double *__restrict__ wave) {
+    tile_update_E<P, V>(g, wave, blockIdx.x, blockIdx.y, blockIdx.z,
+                        blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
+}
+
+template <class P, int V>
+__device__ __forceinline__ void tile_update_H(const GridK &g, const double *__restrict__ wave, int bx, int by, int bz,
+                                              int cta) {
     using T = typename P::T;
     constexpr int N = 3 * V;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0 = (blockIdx.x * g.TZ + tz) * V;
-    const int j = blockIdx.y * g.TY + ty;
-    const int xa = blockIdx.z * g.XC;
+    const int k0 = (bx * g.TZ + tz) * V;
+    const int j = by * g.TY + ty;
+    const int xa = bz * g.XC;
     const int xb = min(nx, xa + g.XC);
     const bool act = (j < ny) && (k0 < nz);
-    const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     const T c = courant_of<T>(g);
     const T *__restrict__ E = (const T *)g.E;
     T *H = (T *)g.H;
@@ -152,6 +160,12 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
 #pragma unroll
         for (int q = 0; q < N; ++q) ec[q] = en[q];
     }
+}
+
+template <class P, int V>
+__global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const double *__restrict__ wave) {
+    tile_update_H<P, V>(g, wave, blockIdx.x, blockIdx.y, blockIdx.z,
+                        blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
 }
 
 // ---------------------------------------------------------------------------

@@ -7,6 +7,7 @@
 
 #include "fdtd_adjoint.cuh"
 #include "fdtd_kernels.cuh"
+#include "fdtd_persistent.cuh"
 #include "fdtd_plan.hpp"
 #include "fdtd_tma.cuh"
 
@@ -262,6 +263,56 @@ static size_t stage_bytes_of(int tile_rows, int mat_E, int mat_H) {
     return a > b ? a : b;
 }
 
+// All steps of a call in one cooperative launch (fdtd_persistent.cuh).
+template <class P>
+static int run_persistent(Plan &p, const fdtd_run_args *a, bool detect, cudaStream_t st) {
+    PersistArgs pa{};
+    pa.n_steps = a->n_steps;
+    pa.wave = a->wave;
+    pa.n_columns = p.n_columns;
+    pa.gz = (int)p.grid.x;
+    pa.gy = (int)p.grid.y;
+    pa.gx = (int)p.grid.z;
+    pa.n_probe = detect ? p.n_probe : 0;
+    pa.probe_cells = p.probe_cells;
+    if (pa.n_probe) {
+        pa.trace_E = (typename P::T *)a->trace_E + a->record_E * 3 * p.n_probe;
+        pa.trace_H = (typename P::T *)a->trace_H + a->record_H * 3 * p.n_probe;
+    }
+    pa.phase = a->phase;
+    pa.n_phase_columns = p.n_phase_columns;
+    pa.n_dft = detect ? (int)p.dft.size() : 0;
+    for (int q = 0; q < pa.n_dft; ++q) pa.dft[q] = p.dft[q];
+    pa.barrier = p.persist_bar;
+    pa.limit = 1u << 23;
+    const bool vec = p.V > 1;
+    const void *fn = vec ? (const void *)k_run_persistent<P, P::V> : (const void *)k_run_persistent<P, 1>;
+    if (p.persist_blocks == 0) {
+        int per_sm = 0, dev = 0, n_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0);
+        if (e != cudaSuccess || per_sm < 1) {
+            set_last_cuda_error((int)e);
+            return FDTD_ERR_CUDA;
+        }
+        p.persist_blocks = per_sm * n_sm;
+    }
+    const int tiles = (int)(p.grid.x * p.grid.y * p.grid.z);
+    const int blocks = std::min(tiles, p.persist_blocks);
+    cudaError_t e = cudaMemsetAsync(p.persist_bar, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess) {
+        GridK gk = p.kf;
+        void *args[] = {&gk, &pa};
+        e = cudaLaunchCooperativeKernel(fn, dim3(blocks), p.block, args, 0, st);
+    }
+    if (e != cudaSuccess) {
+        set_last_cuda_error((int)e);
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
 // n_steps full steps (or one half step).  With capture arguments: detectors
 // and DFTs only when cap->detectors is set, and curl_H on every object box
 // with a capture pointer before each E half (reverse-time adjoint).
@@ -295,6 +346,9 @@ static int run_impl(Plan &p, const fdtd_run_args *a, const fdtd_capture_args *ca
     }
     const GridK &g = p.k;
     const int pblocks = (3 * p.n_probe + kThreads - 1) / kThreads;
+    // small plans: every full step of the call in one cooperative launch
+    if (p.persistent && a->half == 0 && cap == nullptr && a->n_steps >= 2)
+        return run_persistent<P>(p, a, detect, st);
     // one pass per full step (float32 plans that have it), in pairs: the first
     // pass of a pair writes the alternate buffers, the second the caller's; an
     // odd last step runs the two passes

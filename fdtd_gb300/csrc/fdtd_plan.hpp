@@ -69,6 +69,12 @@ struct Plan {
     // direction (0: caller buffers -> alternates, 1: back), their tensor maps
     // (H source, E source, E material, H material) and the launch shape
     int onepass_ok, onepass, onepass_hcopy, onepass_why;
+    // persistent time loop of small register-streaming plans: allowed, used,
+    // its grid-wide barrier counter (device) and resident blocks (0: not yet
+    // looked up)
+    int persist_ok, persistent;
+    unsigned *persist_bar;
+    int persist_blocks;
     GridK ko[2];
     CUtensorMap omaps[2][4];
     dim3 ogrid, oblock;

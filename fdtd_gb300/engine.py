@@ -185,7 +185,9 @@ class Engine:
         # fused-pass kernel choice: variant 0 auto / 1 register streaming / 2 TMA-staged
         # materials: 0 compact copies for the staged passes where possible, 1 full arrays only
         # step_fusion: 0 auto / 1 two passes per step / 2 one pass per step (where allowed)
-        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0, "materials": 0, "step_fusion": 0}
+        # persistent: 0 auto / 1 one launch per half step / 2 one persistent launch per run() (where allowed)
+        self.tuning = {"variant": 0, "tile_rows": 0, "stages": 0, "pml_mode": 0, "materials": 0, "step_fusion": 0,
+                       "persistent": 0}
         self._alt = None  # second buffers of E, H and the PML auxiliaries for one-pass steps
         self.plan = None
         self._key = None
@@ -294,7 +296,7 @@ class Engine:
         self.refresh()
 
     def set_tuning(self, variant=None, tile_rows=None, stages=None, x_chunk=None, pml_mode=None, materials=None,
-                   step_fusion=None):
+                   step_fusion=None, persistent=None):
         """Choose the fused-pass kernels (0 auto, 1 register streaming, 2 TMA-staged),
         the TMA tile rows (4 or 8 with 32-thread-wide tiles, 16 with 16-wide) and
         ring stages, where the PML slabs run
@@ -306,9 +308,11 @@ class Engine:
         currently never, the two-pass plans measured faster; 1 never; 2
         where the grid allows it, else RuntimeError); 0 keeps the automatic
         choice.  The one-pass step uses tile_rows 4 or 8, stages >= 3 and
-        x_chunk when given."""
+        x_chunk when given.  persistent: 0 auto (grids below 8M cells whose
+        plan allows it), 1 one launch per half step, 2 where allowed: every
+        full step of a run() in one cooperative launch."""
         for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode),
-                     ("materials", materials), ("step_fusion", step_fusion)):
+                     ("materials", materials), ("step_fusion", step_fusion), ("persistent", persistent)):
             if v is not None:
                 self.tuning[k] = int(v)
         if x_chunk is not None:
@@ -324,6 +328,10 @@ class Engine:
         info = dict(zip(keys, (int(v) for v in out)))
         info["pml_split"] = info["variant"] // 10
         info["variant"] %= 10
+        # 5: the persistent loop over register-streaming tiles
+        info["persistent"] = int(info["variant"] == 5)
+        if info["persistent"]:
+            info["variant"] = 1
         return info
 
     def check_status(self):
@@ -379,6 +387,7 @@ class Engine:
         d.tile_rows = self.tuning["tile_rows"]
         d.stages = self.tuning["stages"]
         d.pml_mode = self.tuning["pml_mode"]
+        d.persistent = self.tuning["persistent"]
         d.courant = g.courant_number
         d.E, d.H = g._E.data_ptr(), g._H.data_ptr()
         d.E_lo = g._E_lo.data_ptr() if g._E_lo is not None else None

@@ -201,7 +201,13 @@ typedef struct {
      * where the grid allows it.  fdtd_plan_step_fusion reports whether a grid allows it (before any
      * buffer is allocated), whether the plan uses it, and why not. */
     int32_t step_fusion;
-    int32_t reserved_fusion;
+    /* Persistent time loop (ABI 5): on small grids whose plan runs the
+     * register-streaming passes with nothing between them but detector
+     * gathers and DFT sums, fdtd_run runs all full steps of a call in one
+     * cooperative launch whose blocks meet at a grid-wide barrier between
+     * half steps (bounded waits: bit 2 of the status word on expiry).  0
+     * automatic (grids below 8M cells), 1 off, 2 on where the plan allows it. */
+    int32_t persistent;
     void *E_alt;
     void *H_alt;
     void *psi_alt[FDTD_MAX_BOUNDARIES][2]; /* per PML boundary: second psi_E, psi_H; NULL for periodic */
@@ -240,7 +246,8 @@ int fdtd_plan_destroy(fdtd_plan *plan);
  * stream: 0 = healthy; bit 0 = a staged kernel's pipeline wait expired (the
  * step's results are invalid); bit 1 = besides, a CTA gave up waiting for its
  * own copies in flight (results of later kernels on this context are
- * untrusted too).  reset != 0 clears the word afterwards.  No
+ * untrusted too); bit 2 = a persistent run's grid-wide barrier wait expired
+ * (the run's results are invalid).  reset != 0 clears the word afterwards.  No
  * reference counterpart (the reference cannot fail this way). */
 int fdtd_plan_status(fdtd_plan *plan, int32_t *out, int32_t reset, fdtd_stream_t stream);
 
@@ -369,7 +376,8 @@ int fdtd_plan_step_fusion(const fdtd_plan *plan, int32_t *allowed, int32_t *acti
  * threads along z, rows along y, planes along x per CTA, CTAs, kernels per
  * full step, variant (1 register streaming, 2 TMA-staged; plus 10 when the
  * PML slabs run in kernels of their own; 4 one pass per full step, whose
- * tiling is then reported), ring stages. */
+ * tiling is then reported; 5 the persistent loop of register-streaming
+ * tiles, one launch per fdtd_run call), ring stages. */
 int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8);
 
 const char *fdtd_status_string(int32_t status);
