@@ -244,6 +244,37 @@ __device__ __forceinline__ void ld_vec_ro(T (&dst)[N], const T *__restrict__ p) 
     }
 }
 
+// Load cached in L2 only: for data that other blocks of the same launch
+// write (the persistent time loop), which L1 could hold stale copies of.
+template <class T, int N>
+__device__ __forceinline__ void ld_vec_cg(T (&dst)[N], const T *p) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+        for (int i = 0; i < (int)(N * sizeof(T) / 16); ++i) {
+            uint4 t = __ldcg(q + i);
+            *reinterpret_cast<uint4 *>(&dst[i * 16 / sizeof(T)]) = t;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) dst[i] = __ldcg(p + i);
+    }
+}
+
+// Field loads of the register-streaming tiles: the read-only path (CG =
+// false, one launch per half step) or L2 only (CG = true, persistent loop).
+template <bool CG, class T, int N>
+__device__ __forceinline__ void ld_field(T (&dst)[N], const T *p) {
+    if constexpr (CG) ld_vec_cg(dst, p);
+    else ld_vec_ro(dst, p);
+}
+
+template <bool CG, class T>
+__device__ __forceinline__ T ld_field1(const T *p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
+
 template <class T, int N>
 __device__ __forceinline__ void st_vec(T *p, const T (&src)[N]) {
     if constexpr ((N * sizeof(T)) % 16 == 0) {

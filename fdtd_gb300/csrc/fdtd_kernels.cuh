@@ -23,7 +23,9 @@ namespace fdtd {
 // kernels do not take (nz not a multiple of the vector width, unaligned data).
 // One tile of the E half (bx, by, bz: tile coordinates; cta: its index in the
 // per-CTA lists), for the one-tile-per-block kernel and the persistent one.
-template <class P, int V>
+// CG: the other half's field is written by other blocks of the same launch
+// (persistent loop), so it is loaded through L2 only, not the read-only path.
+template <class P, int V, bool CG = false>
 __device__ __forceinline__ void tile_update_E(const GridK &g, const double *__restrict__ wave, int bx, int by, int bz,
                                               int cta) {
     using T = typename P::T;
@@ -52,7 +54,7 @@ __device__ __forceinline__ void tile_update_E(const GridK &g, const double *__re
     alignas(16) T hp[N];  // H at plane i-1
 #pragma unroll
     for (int q = 0; q < N; ++q) hp[q] = T(0);
-    if (act && xa > 0) ld_vec_ro(hp, H + 3 * (((size_t)(xa - 1) * ny + j) * nz + k0));
+    if (act && xa > 0) ld_field<CG>(hp, H + 3 * (((size_t)(xa - 1) * ny + j) * nz + k0));
 
     for (int i = xa; i < xb; ++i) {
         const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
@@ -66,8 +68,8 @@ __device__ __forceinline__ void tile_update_E(const GridK &g, const double *__re
             m[q] = T(0);
         }
         if (act) {
-            ld_vec_ro(hc, H + 3 * cell0);
-            if (j > 0) ld_vec_ro(hj, H + 3 * (cell0 - nz));
+            ld_field<CG>(hc, H + 3 * cell0);
+            if (j > 0) ld_field<CG>(hj, H + 3 * (cell0 - nz));
             ld_vec(e, E + 3 * cell0);
             if constexpr (P::COMP) ld_vec(el, Elo + 3 * cell0);
             ld_vec_ro(m, IE + 3 * cell0);
@@ -76,8 +78,8 @@ __device__ __forceinline__ void tile_update_E(const GridK &g, const double *__re
         T kx = __shfl_up_sync(FULL_MASK, hc[N - 3], 1);
         T ky = __shfl_up_sync(FULL_MASK, hc[N - 2], 1);
         if (tz == 0 && act && k0 > 0) {
-            kx = H[3 * (cell0 - 1)];
-            ky = H[3 * (cell0 - 1) + 1];
+            kx = ld_field1<CG>(H + 3 * (cell0 - 1));
+            ky = ld_field1<CG>(H + 3 * (cell0 - 1) + 1);
         }
         if (act) {
             const unsigned slabs = mask_yz | slab_mask_x(g, i);
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(kThreads) k_update_E(const GridK g, const doub
                         blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
 }
 
-template <class P, int V>
+template <class P, int V, bool CG = false>
 __device__ __forceinline__ void tile_update_H(const GridK &g, const double *__restrict__ wave, int bx, int by, int bz,
                                               int cta) {
     using T = typename P::T;
@@ -124,7 +126,7 @@ __device__ __forceinline__ void tile_update_H(const GridK &g, const double *__re
     alignas(16) T ec[N];  // E at plane i
 #pragma unroll
     for (int q = 0; q < N; ++q) ec[q] = T(0);
-    if (act && xa < xb) ld_vec_ro(ec, E + 3 * (((size_t)xa * ny + j) * nz + k0));
+    if (act && xa < xb) ld_field<CG>(ec, E + 3 * (((size_t)xa * ny + j) * nz + k0));
 
     for (int i = xa; i < xb; ++i) {
         const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
@@ -138,8 +140,8 @@ __device__ __forceinline__ void tile_update_H(const GridK &g, const double *__re
             m[q] = T(0);
         }
         if (act) {
-            if (i + 1 < nx) ld_vec_ro(en, E + 3 * (cell0 + (size_t)ny * nz));
-            if (j + 1 < ny) ld_vec_ro(ej, E + 3 * (cell0 + nz));
+            if (i + 1 < nx) ld_field<CG>(en, E + 3 * (cell0 + (size_t)ny * nz));
+            if (j + 1 < ny) ld_field<CG>(ej, E + 3 * (cell0 + nz));
             ld_vec(h, H + 3 * cell0);
             if constexpr (P::COMP) ld_vec(hl, Hlo + 3 * cell0);
             ld_vec_ro(m, MU + 3 * cell0);
@@ -148,8 +150,8 @@ __device__ __forceinline__ void tile_update_H(const GridK &g, const double *__re
         T kx = __shfl_down_sync(FULL_MASK, ec[0], 1);
         T ky = __shfl_down_sync(FULL_MASK, ec[1], 1);
         if (tz == g.TZ - 1 && act && k0 + V < nz) {
-            kx = E[3 * (cell0 + V)];
-            ky = E[3 * (cell0 + V) + 1];
+            kx = ld_field1<CG>(E + 3 * (cell0 + V));
+            ky = ld_field1<CG>(E + 3 * (cell0 + V) + 1);
         }
         if (act) {
             const unsigned slabs = mask_yz | slab_mask_x(g, i);

@@ -11,6 +11,9 @@
 // DFT accumulation of a half step run after its barrier, interleaved with the
 // next half step (which never writes the field they read).
 //
+// Fields the other half step wrote are read with L2-only loads (the
+// read-only path may keep lines in L1 across the barrier).
+//
 // The launch is cooperative (all blocks resident at once, so the barrier
 // cannot wait for a block that never runs).  Barrier waits are bounded: a
 // block that gives up sets bit 2 of the plan's status word and returns, and
@@ -103,7 +106,7 @@ __global__ void __launch_bounds__(kThreads) k_run_persistent(const GridK g, cons
         const double *wave = a.n_columns > 0 ? a.wave + s * a.n_columns : nullptr;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int bx = t % a.gz, by = (t / a.gz) % a.gy, bz = t / (a.gz * a.gy);
-            tile_update_E<P, V>(g, wave, bx, by, bz, t);
+            tile_update_E<P, V, true>(g, wave, bx, by, bz, t);
         }
         if (!grid_barrier(a.barrier, ++epoch, a.limit, g.status)) return;
         // E is final for this step: gathers and DFT overlap the H half
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(kThreads) k_run_persistent(const GridK g, cons
             persist_dft<T, P::COMP>(g, a.dft[d], a.phase + s * 2 * a.n_phase_columns, tid, nthr);
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int bx = t % a.gz, by = (t / a.gz) % a.gy, bz = t / (a.gz * a.gy);
-            tile_update_H<P, V>(g, wave, bx, by, bz, t);
+            tile_update_H<P, V, true>(g, wave, bx, by, bz, t);
         }
         if (!grid_barrier(a.barrier, ++epoch, a.limit, g.status)) return;
         if (a.n_probe) {
