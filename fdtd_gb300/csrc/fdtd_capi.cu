@@ -658,12 +658,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     build_csr(t, items, srcE0, d->n_sources_E, se_off, se_idx);
     build_csr(t, items, srcH0, d->n_sources_H, sh_off, sh_idx);
 
-    // Launch order of the staged passes: the tiles that carry more work per
+    // Launch order of the staged passes (and tile order of the persistent
+    // loop over register-streaming tiles): the tiles that carry more work per
     // plane (object cells, weighted by the coefficient values they read, and
     // cells of the PML slabs inside the fused pass) first, so that they run
     // in the first waves instead of finishing last; the rest in grid order.
     std::vector<int> cta_order;
-    if (p.variant == 2) {
+    {
         const long ncta = (long)t.gz * t.gy * t.gx;
         const int zc = t.V * t.TZ;
         std::vector<double> extra(ncta, 0.0);
@@ -907,7 +908,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                                                 ose_off.size() + ose_idx.size() + osh_off.size() + osh_idx.size() +
                                                 cta_order.size() + 13));
     const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
-    const size_t b_status = 512;  // status word, then the persistent loop's barrier counter
+    const size_t b_status = 512;  // status word; at +256 the persistent loop's barrier and tile counters
     std::vector<char> host(b_items + b_lists + b_runs + b_status, 0);
     if (nitems) memcpy(host.data(), items.data(), sizeof(ItemK) * nitems);
     int *lists = (int *)(host.data() + b_items);
@@ -951,10 +952,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.srcE_idx = dl + at_se_idx;
     g.srcH_off = dl + at_sh_off;
     g.srcH_idx = dl + at_sh_idx;
-    g.cta_order = cta_order.empty() ? nullptr : dl + at_order;
+    const int *order = cta_order.empty() ? nullptr : dl + at_order;
+    g.cta_order = p.variant == 2 ? order : nullptr;
+    p.persist_order = p.variant == 1 ? order : nullptr;
     p.runs = (const int2 *)(base + b_items + b_lists);
     g.status = (int *)(base + b_items + b_lists + b_runs);
     p.persist_bar = (unsigned *)(base + b_items + b_lists + b_runs + 256);
+    p.persist_tickets = (unsigned long long *)(base + b_items + b_lists + b_runs + 264);
     if (p.variant == 2) {
         const int rc = d->precision == FDTD_FLOAT32    ? prepare_tma_f32(p)
                        : d->precision == FDTD_FLOAT32C ? prepare_tma_f32c(p)

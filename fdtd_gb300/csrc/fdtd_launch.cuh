@@ -284,6 +284,8 @@ static int run_persistent(Plan &p, const fdtd_run_args *a, bool detect, cudaStre
     pa.n_dft = detect ? (int)p.dft.size() : 0;
     for (int q = 0; q < pa.n_dft; ++q) pa.dft[q] = p.dft[q];
     pa.barrier = p.persist_bar;
+    pa.tickets = p.persist_tickets;
+    pa.order = p.persist_order;
     pa.limit = 1u << 23;
     const bool vec = p.V > 1;
     const void *fn = vec ? (const void *)k_run_persistent<P, P::V> : (const void *)k_run_persistent<P, 1>;
@@ -300,7 +302,8 @@ static int run_persistent(Plan &p, const fdtd_run_args *a, bool detect, cudaStre
     }
     const int tiles = (int)(p.grid.x * p.grid.y * p.grid.z);
     const int blocks = std::min(tiles, p.persist_blocks);
-    cudaError_t e = cudaMemsetAsync(p.persist_bar, 0, sizeof(unsigned), st);
+    // the barrier counter and, 8 bytes on, the ticket counter
+    cudaError_t e = cudaMemsetAsync(p.persist_bar, 0, 16, st);
     if (e == cudaSuccess) {
         GridK gk = p.kf;
         void *args[] = {&gk, &pa};

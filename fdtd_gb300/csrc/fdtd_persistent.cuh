@@ -4,7 +4,7 @@
 // A grid of a few million cells takes tens of microseconds per half step, so
 // a run of two launches per step (plus detector gathers) is bound by launch
 // latency and by the partly filled last wave of each launch rather than by
-// memory.  Here every block loops over the register-streaming tiles of a
+// memory.  Here the blocks share out the register-streaming tiles of a
 // half step (tile_update_E / tile_update_H, the same per-cell arithmetic as
 // the one-launch-per-half-step plan, so the same bits), then all blocks meet
 // at a grid-wide barrier before the other half step.  Detector gathers and
@@ -39,8 +39,10 @@ struct PersistArgs {
     int n_phase_columns;
     int n_dft;
     fdtd_dft_desc dft[kPersistMaxDft];
-    unsigned *barrier;  // arrival counter, zero at launch
-    unsigned limit;     // polls before a barrier wait gives up
+    unsigned *barrier;                // arrival counter, zero at launch
+    unsigned long long *tickets;      // tile tickets drawn, zero at launch
+    const int *order;                 // tile of each ticket, heaviest first (null: grid order)
+    unsigned limit;                   // polls before a barrier wait gives up
 };
 
 // Grid-wide barrier number `epoch` (1, 2, ...): the counter counts every
@@ -95,19 +97,48 @@ __device__ __forceinline__ void persist_dft(const GridK &g, const fdtd_dft_desc 
     }
 }
 
+// The tiles of one half step, handed out by ticket: every block draws tickets
+// from one counter until it draws one past the last tile, so a block that got
+// light tiles takes more of them and the half step ends with no block left
+// holding a queue of its own.  Each block draws exactly one ticket past the
+// end, so half step h owns tickets [h (ntiles + blocks), (h + 1) (ntiles +
+// blocks)) and the counter never needs resetting between half steps.  The next
+// ticket is drawn before the current tile runs, hiding the atomic's latency.
+template <bool IS_E, class P, int V>
+__device__ __forceinline__ void persist_half(const GridK &g, const PersistArgs &a, const double *wave, int ntiles,
+                                             unsigned long long base) {
+    __shared__ int ticket_s;
+    const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+    if (lead) ticket_s = (int)(atomicAdd(a.tickets, 1ull) - base);
+    __syncthreads();
+    int t = ticket_s;
+    while (t < ntiles) {
+        unsigned long long next = 0;
+        if (lead) next = atomicAdd(a.tickets, 1ull);
+        const int tile = a.order ? a.order[t] : t;
+        const int bx = tile % a.gz, by = (tile / a.gz) % a.gy, bz = tile / (a.gz * a.gy);
+        if constexpr (IS_E) tile_update_E<P, V, true>(g, wave, bx, by, bz, tile);
+        else tile_update_H<P, V, true>(g, wave, bx, by, bz, tile);
+        __syncthreads();  // every thread has read ticket_s
+        if (lead) ticket_s = (int)(next - base);
+        __syncthreads();
+        t = ticket_s;
+    }
+}
+
 template <class P, int V>
 __global__ void __launch_bounds__(kThreads) k_run_persistent(const GridK g, const PersistArgs a) {
     using T = typename P::T;
     const int ntiles = a.gz * a.gy * a.gx;
     const long nthr = (long)gridDim.x * kThreads;
     const long tid = (long)blockIdx.x * kThreads + threadIdx.y * blockDim.x + threadIdx.x;
+    const unsigned long long per_half = (unsigned long long)ntiles + gridDim.x;
+    unsigned long long base = 0;
     unsigned epoch = 0;
     for (long long s = 0; s < a.n_steps; ++s) {
         const double *wave = a.n_columns > 0 ? a.wave + s * a.n_columns : nullptr;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            const int bx = t % a.gz, by = (t / a.gz) % a.gy, bz = t / (a.gz * a.gy);
-            tile_update_E<P, V, true>(g, wave, bx, by, bz, t);
-        }
+        persist_half<true, P, V>(g, a, wave, ntiles, base);
+        base += per_half;
         if (!grid_barrier(a.barrier, ++epoch, a.limit, g.status)) return;
         // E is final for this step: gathers and DFT overlap the H half
         if (a.n_probe) {
@@ -116,10 +147,8 @@ __global__ void __launch_bounds__(kThreads) k_run_persistent(const GridK g, cons
         }
         for (int d = 0; d < a.n_dft; ++d)
             persist_dft<T, P::COMP>(g, a.dft[d], a.phase + s * 2 * a.n_phase_columns, tid, nthr);
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            const int bx = t % a.gz, by = (t / a.gz) % a.gy, bz = t / (a.gz * a.gy);
-            tile_update_H<P, V, true>(g, wave, bx, by, bz, t);
-        }
+        persist_half<false, P, V>(g, a, wave, ntiles, base);
+        base += per_half;
         if (!grid_barrier(a.barrier, ++epoch, a.limit, g.status)) return;
         if (a.n_probe) {
             T *out = (T *)a.trace_H + s * 3 * a.n_probe;

@@ -70,10 +70,13 @@ struct Plan {
     // (H source, E source, E material, H material) and the launch shape
     int onepass_ok, onepass, onepass_hcopy, onepass_why;
     // persistent time loop of small register-streaming plans: allowed, used,
-    // its grid-wide barrier counter (device) and resident blocks (0: not yet
+    // its grid-wide barrier and tile-ticket counters (device), the tile order
+    // (heaviest first; null: grid order) and resident blocks (0: not yet
     // looked up)
     int persist_ok, persistent;
     unsigned *persist_bar;
+    unsigned long long *persist_tickets;
+    const int *persist_order;
     int persist_blocks;
     GridK ko[2];
     CUtensorMap omaps[2][4];
