@@ -97,30 +97,33 @@ __device__ __forceinline__ void persist_dft(const GridK &g, const fdtd_dft_desc 
     }
 }
 
-// The tiles of one half step, handed out by ticket: every block draws tickets
-// from one counter until it draws one past the last tile, so a block that got
-// light tiles takes more of them and the half step ends with no block left
-// holding a queue of its own.  Each block draws exactly one ticket past the
-// end, so half step h owns tickets [h (ntiles + blocks), (h + 1) (ntiles +
-// blocks)) and the counter never needs resetting between half steps.  The next
-// ticket is drawn before the current tile runs, hiding the atomic's latency.
+// The tiles of one half step: each block's first tile is its own (the
+// heaviest tiles go to the first blocks), the rest are handed out by ticket:
+// a block draws tickets from one counter until it draws one past the last
+// tile, so a block that got light tiles takes more of them and the half step
+// ends with no block left holding a queue of its own.  Each block draws
+// exactly one ticket past the end, so half step h owns tickets [h ntiles,
+// (h + 1) ntiles) and the counter never needs resetting.  A block draws its
+// next ticket before its current tile runs, hiding the atomic's latency.
+// With no more tiles than blocks nothing is drawn.
 template <bool IS_E, class P, int V>
 __device__ __forceinline__ void persist_half(const GridK &g, const PersistArgs &a, const double *wave, int ntiles,
                                              unsigned long long base) {
     __shared__ int ticket_s;
     const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
-    if (lead) ticket_s = (int)(atomicAdd(a.tickets, 1ull) - base);
-    __syncthreads();
-    int t = ticket_s;
+    const int nblk = (int)gridDim.x;
+    const bool draw = ntiles > nblk;
+    int t = blockIdx.x;
     while (t < ntiles) {
         unsigned long long next = 0;
-        if (lead) next = atomicAdd(a.tickets, 1ull);
+        if (lead && draw) next = atomicAdd(a.tickets, 1ull);
         const int tile = a.order ? a.order[t] : t;
         const int bx = tile % a.gz, by = (tile / a.gz) % a.gy, bz = tile / (a.gz * a.gy);
         if constexpr (IS_E) tile_update_E<P, V, true>(g, wave, bx, by, bz, tile);
         else tile_update_H<P, V, true>(g, wave, bx, by, bz, tile);
+        if (!draw) break;
         __syncthreads();  // every thread has read ticket_s
-        if (lead) ticket_s = (int)(next - base);
+        if (lead) ticket_s = nblk + (int)(next - base);
         __syncthreads();
         t = ticket_s;
     }
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kThreads) k_run_persistent(const GridK g, cons
     const int ntiles = a.gz * a.gy * a.gx;
     const long nthr = (long)gridDim.x * kThreads;
     const long tid = (long)blockIdx.x * kThreads + threadIdx.y * blockDim.x + threadIdx.x;
-    const unsigned long long per_half = (unsigned long long)ntiles + gridDim.x;
+    const unsigned long long per_half = ntiles > (int)gridDim.x ? (unsigned long long)ntiles : 0ull;
     unsigned long long base = 0;
     unsigned epoch = 0;
     for (long long s = 0; s < a.n_steps; ++s) {
