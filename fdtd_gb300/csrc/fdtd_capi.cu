@@ -1049,7 +1049,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         p.persist_ok = coop && p.variant == 1 && p.epi_E.empty() && p.epi_H.empty() && !p.has_feedback &&
                        p.n_current == 0 && (int)p.dft.size() <= kPersistMaxDft;
-        p.persistent = p.persist_ok && (d->persistent == 2 || (d->persistent == 0 && ncell < (8L << 20)));
+        // automatic: float32 below 3M cells, float64 below 8M (measured
+        // against one launch per half step, register tiles, 500 steps: 64^3
+        // with a 10-cell PML 1.54x float32 / 1.25x float64; 128^3 with PML
+        // and objects 1.03-1.12x; 192x192x96 with PML and an anisotropic box
+        // 0.985x float32, 1.07x float64)
+        const long auto_cells = d->precision == FDTD_FLOAT64 ? (8L << 20) : 3000000L;
+        p.persistent = p.persist_ok && (d->persistent == 2 || (d->persistent == 0 && ncell < auto_cells));
         p.persist_blocks = 0;
     }
     p.stats_ctas = std::max(1, std::min(4 * n_sm, FDTD_STATS_STATIC_MAX_ROWS));

@@ -308,8 +308,8 @@ class Engine:
         currently never, the two-pass plans measured faster; 1 never; 2
         where the grid allows it, else RuntimeError); 0 keeps the automatic
         choice.  The one-pass step uses tile_rows 4 or 8, stages >= 3 and
-        x_chunk when given.  persistent: 0 auto (grids below 8M cells whose
-        plan allows it), 1 one launch per half step, 2 where allowed: every
+        x_chunk when given.  persistent: 0 auto (float32 grids below 3M
+        cells, float64 below 8M, whose plan allows it), 1 one launch per half step, 2 where allowed: every
         full step of a run() in one cooperative launch."""
         for k, v in (("variant", variant), ("tile_rows", tile_rows), ("stages", stages), ("pml_mode", pml_mode),
                      ("materials", materials), ("step_fusion", step_fusion), ("persistent", persistent)):

@@ -206,7 +206,8 @@ typedef struct {
      * gathers and DFT sums, fdtd_run runs all full steps of a call in one
      * cooperative launch whose blocks meet at a grid-wide barrier between
      * half steps (bounded waits: bit 2 of the status word on expiry).  0
-     * automatic (grids below 8M cells), 1 off, 2 on where the plan allows it. */
+     * automatic (float32 grids below 3M cells, float64 below 8M), 1 off, 2 on
+     * where the plan allows it. */
     int32_t persistent;
     void *E_alt;
     void *H_alt;
