@@ -253,7 +253,11 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                aligned16(d->inv_mu) && (!comp || (aligned16(d->E_lo) && aligned16(d->H_lo)));
     if (d->variant < 0 || d->variant > 2) return FDTD_ERR_ARGUMENT;
     if (d->variant == 2 && !vec) return FDTD_ERR_UNSUPPORTED;
-    if (d->pml_mode < 0 || d->pml_mode > 3) return FDTD_ERR_ARGUMENT;
+    if (d->pml_mode < 0 || d->pml_mode > 5) return FDTD_ERR_ARGUMENT;
+    // modes 4 and 5: modes 3 and 1 with the auxiliaries of x/y slabs read
+    // in-lane from global memory instead of staged through the ring
+    const int pml_base = d->pml_mode == 4 ? 3 : (d->pml_mode == 5 ? 1 : d->pml_mode);
+    g.psi_direct = d->pml_mode >= 4;
     // PML slabs in kernels of their own let the fused pass run without slab
     // work (the staged kernels reach the HBM roofline there); the slab kernels
     // re-read only the slab cells.  The per-cell order of the reference is
@@ -278,13 +282,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // 2D grids (nz = 1) of 8M cells and more split too (8192^2 float32: 63.1
     // vs 58.0 Gcell/s with 32-plane chunks)
     p.pml_split = g.nslab > 0 &&
-                  (d->pml_mode >= 2 ||
-                   (d->pml_mode == 0 && ncell >= (8L << 20) &&
+                  (pml_base >= 2 ||
+                   (pml_base == 0 && ncell >= (8L << 20) &&
                     ((vec && (long)d->nz * 3 * (long)esize >= 768) || d->nz == 1)));
     int kfs = 0;  // leading slabs kept in the fused pass when split
-    const bool auto_keep = d->pml_mode == 0 && d->precision == FDTD_FLOAT32 && mat_want[0] != MAT_FULL &&
+    const bool auto_keep = pml_base == 0 && d->precision == FDTD_FLOAT32 && mat_want[0] != MAT_FULL &&
                            mat_want[1] != MAT_FULL;
-    if (p.pml_split && (d->pml_mode == 3 || auto_keep)) {
+    if (p.pml_split && (pml_base == 3 || auto_keep)) {
         while (kfs < d->n_boundaries && d->boundaries[kfs].kind == FDTD_BOUNDARY_PML &&
                (auto_keep ? d->boundaries[kfs].axis == 1 : d->boundaries[kfs].axis != 2))
             ++kfs;
@@ -312,6 +316,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.epi_H = p.epi_E;
     }
     const int ks = p.pml_split ? kfs : g.nslab;  // slabs the fused pass handles
+    g.n_staged = 0;
+    for (int s = 0; s < ks; ++s)
+        if (!g.psi_direct || g.slab[s].axis == 2) g.staged_slab[g.n_staged++] = s;
     // automatic choice: the TMA-staged kernels reach the HBM roofline on grids
     // without PML; with PML slabs the warps holding slab cells do more work per
     // plane and the staged kernels' per-plane CTA barrier makes the whole tile
@@ -351,6 +358,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             int slot_of[kMaxSlabs] = {0};
             for (int s = 0; s < ks; ++s) {
                 const SlabK &S = g.slab[s];
+                if (g.psi_direct && S.axis != 2) continue;  // read in-lane, no slot
                 const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? TY : Zc);
                 const std::pair<int, int> rg(S.start / unit, (S.start + S.th - 1) / unit);
                 const int pitch = S.axis == 2 ? 2 * S.thp : 2 * Zc;
@@ -377,7 +385,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 sl.off = stage;
                 stage += (sl.bytes + 127) & ~(size_t)127;
             }
-            for (int s = 0; s < ks; ++s) (off_out ? off_out : g.psi_off)[s] = (int)slots[slot_of[s]].off;
+            for (int s = 0; s < ks; ++s)
+                if (!g.psi_direct || g.slab[s].axis == 2)
+                    (off_out ? off_out : g.psi_off)[s] = (int)slots[slot_of[s]].off;
             return stage;
         };
         int coef = 0;
@@ -408,8 +418,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         // drop (one-byte material indices): two CTAs per SM measured 77 vs
         // 67 Gcell/s on config 3 (float32) and 15.2 vs 12.6 (float64), and
         // the same as one CTA with full material arrays
+        int staged_slabs = 0;  // slabs whose auxiliary rows the stage holds
+        for (int s = 0; s < ks; ++s) staged_slabs += !g.psi_direct || g.slab[s].axis == 2;
         int rows = d->tile_rows;
-        if (rows == 16 && ks > 4) {
+        if (rows == 16 && staged_slabs > 4) {
             if (d->variant == 2) return FDTD_ERR_UNSUPPORTED;
             rows = 8;
         }
@@ -417,7 +429,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             const long z32 = 32L * vmax, z16 = 16L * vmax;
             const long waste32 = (d->nz + z32 - 1) / z32 * z32 - d->nz;
             const long waste16 = (d->nz + z16 - 1) / z16 * z16 - d->nz;
-            if (waste16 < waste32 && ks <= 4) {
+            if (waste16 < waste32 && staged_slabs <= 4) {
                 rows = 16;
             } else {
                 rows = 8;
@@ -988,6 +1000,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             GridK &k = p.ko[dir];
             k = p.k;
             k.nslab_fused = k.nslab;
+            k.psi_direct = 0;  // the one-pass stage holds every slab's auxiliary rows
             k.TZ = kl.TZ;
             k.TY = kl.TY;
             k.XC = kl.XC;

@@ -249,7 +249,7 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
         else gofs = ((long)i * g.ny + j) * S.thp + l0;
         T *gp = psi + 2 * gofs;
         const T *sp = nullptr;
-        if (src.stage)
+        if (src.stage && (a == 2 || !g.psi_direct))
             sp = reinterpret_cast<const T *>(src.stage + (HOFF ? g.psi_offH[s] : g.psi_off[s])) +
                  src.row * (HOFF ? g.psi_pitchH[s] : g.psi_pitch[s]) + (a == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
         T bu = T(0), cu = T(0);  // coefficients when l is the same for the V cells

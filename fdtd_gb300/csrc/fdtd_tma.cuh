@@ -127,7 +127,7 @@ struct StageGeom {
 };
 
 // Fill one stage for plane p (warp 0 of the CTA, all lanes).  The PML auxiliary rows of
-// every slab crossing the tile at plane p are copied with 1D bulk copies (one
+// every staged slab crossing the tile at plane p are copied with 1D bulk copies (one
 // row per lane), then lane 0 arms the stage barrier with the total byte count
 // and issues the field tiles.
 template <class T, int TY>
@@ -143,9 +143,10 @@ __device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, ui
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int q = lane + 32 * h;
-        const int s = q / TY, rr = q % TY;
+        const int si = q / TY, rr = q % TY;
         const int j = j0 + rr;
-        if (!with_psi || s >= g.nslab || j >= g.ny) continue;
+        if (!with_psi || si >= g.n_staged || j >= g.ny) continue;
+        const int s = g.staged_slab[si];
         const SlabK &S = g.slab[s];
         const T *psi = (const T *)(is_E ? S.psiE_rd : S.psiH_rd);
         const int cells = min(Zc, g.nz - k0c);
