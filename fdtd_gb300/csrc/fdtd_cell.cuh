@@ -228,41 +228,43 @@ __device__ __forceinline__ void pml_correct(typename P::T &f, typename P::T &fl,
 // updated auxiliaries (a neighbour's cell recomputed by the one-pass step);
 // HOFF selects the stage's H-side auxiliary slots (g.psi_offH/psi_pitchH) of
 // the one-pass step instead of g.psi_off/psi_pitch.
-template <class P, int V, bool IS_E, bool HOFF = false>
-__device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, typename P::T c,
-                                          const typename P::T (&d)[6][V], const typename P::T (&m)[3 * V],
-                                          typename P::T (&f)[3 * V], typename P::T (&fl)[3 * V],
-                                          const PsiSrc<typename P::T> &src, unsigned slabs, bool store = true) {
+template <class P, int V, bool IS_E, bool HOFF, int A>
+__device__ __forceinline__ void apply_pml_slab(const GridK &g, int s, int i, int j, int k0, typename P::T c,
+                                               const typename P::T (&d)[6][V], const typename P::T (&m)[3 * V],
+                                               typename P::T (&f)[3 * V], typename P::T (&fl)[3 * V],
+                                               const PsiSrc<typename P::T> &src, bool store) {
     using T = typename P::T;
-    for (unsigned sm = slabs; sm; sm &= sm - 1) {
-        const int s = __ffs(sm) - 1;
-        const SlabK &S = g.slab[s];
-        const int a = S.axis, th = S.th;
-        T *psi = (T *)(IS_E ? S.psiE : S.psiH);
-        const T *bt = (const T *)(IS_E ? S.bE : S.bH);
-        const T *ct = (const T *)(IS_E ? S.cE : S.cH);
-        // slab-local index of cell k0 and the rows of its auxiliaries
-        const int l0 = (a == 0 ? i : (a == 1 ? j : k0)) - S.start;
-        long gofs;
-        if (a == 0) gofs = ((long)l0 * g.ny + j) * g.nz + k0;
-        else if (a == 1) gofs = ((long)i * th + l0) * g.nz + k0;
-        else gofs = ((long)i * g.ny + j) * S.thp + l0;
-        T *gp = psi + 2 * gofs;
-        const T *sp = nullptr;
-        if (src.stage && (a == 2 || !g.psi_direct))
-            sp = reinterpret_cast<const T *>(src.stage + (HOFF ? g.psi_offH[s] : g.psi_off[s])) +
-                 src.row * (HOFF ? g.psi_pitchH[s] : g.psi_pitch[s]) + (a == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
-        T bu = T(0), cu = T(0);  // coefficients when l is the same for the V cells
-        if (a != 2) {
-            bu = src.ctab ? src.ctab[g.coef_off[s] + l0] : bt[l0];
-            cu = src.ctab ? src.ctab[g.coef_off[s] + th + l0] : ct[l0];
-        }
-        const bool corr = s < g.nslab_fused;
-        // all loads first (a store to the auxiliaries would otherwise order every
-        // later load behind it), then the updates, then the stores
-        T p0[V], p1[V];
-        if (V > 1 && a != 2) {
-            // x/y slab: the V cells are one contiguous, 16-byte aligned run of pairs
+    const SlabK &S = g.slab[s];
+    const int th = S.th;
+    T *psi = (T *)(IS_E ? S.psiE : S.psiH);
+    const T *bt = (const T *)(IS_E ? S.bE : S.bH);
+    const T *ct = (const T *)(IS_E ? S.cE : S.cH);
+    // slab-local index of cell k0 and the rows of its auxiliaries
+    const int l0 = (A == 0 ? i : (A == 1 ? j : k0)) - S.start;
+    long gofs;
+    if constexpr (A == 0) gofs = ((long)l0 * g.ny + j) * g.nz + k0;
+    else if constexpr (A == 1) gofs = ((long)i * th + l0) * g.nz + k0;
+    else gofs = ((long)i * g.ny + j) * S.thp + l0;
+    T *gp = psi + 2 * gofs;
+    const T *sp = nullptr;
+    if (src.stage && (A == 2 || !g.psi_direct))
+        sp = reinterpret_cast<const T *>(src.stage + (HOFF ? g.psi_offH[s] : g.psi_off[s])) +
+             src.row * (HOFF ? g.psi_pitchH[s] : g.psi_pitch[s]) + (A == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
+    const T *tb = src.ctab ? src.ctab + g.coef_off[s] : bt;  // b at [l], c at [th + l] (shared) or ct[l]
+    const T *tc = src.ctab ? src.ctab + g.coef_off[s] + th : ct;
+    const bool corr = s < g.nslab_fused;
+    // phi[(A+1)%3] = -p0, phi[(A+2)%3] = +p1 (fdtd/boundaries.py:457-459, 485-487);
+    // p0 is driven by the difference d0, p1 by d1
+    constexpr int q0 = A == 0 ? 1 : (A == 1 ? 2 : 5);
+    constexpr int q1 = A == 0 ? 0 : (A == 1 ? 3 : 4);
+    constexpr int c0 = (A + 1) % 3, c1 = (A + 2) % 3;
+    // all loads first (a store to the auxiliaries would otherwise order every
+    // later load behind it), then the updates, then the stores
+    T p0[V], p1[V];
+    if constexpr (A != 2) {
+        // x/y slab: the V cells share one slab-local index
+        if constexpr (V > 1) {
+            // one contiguous, 16-byte aligned run of pairs
             alignas(16) T pr[2 * V];
             if (sp) ld_vec(pr, sp);
             else ld_vec(pr, (const T *)gp);
@@ -272,56 +274,33 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
                 p1[v] = pr[2 * v + 1];
             }
         } else {
+            const T *q = sp ? sp : gp;
+            p0[0] = q[0];
+            p1[0] = q[1];
+        }
+        const T b = tb[l0], cc = tc[l0];
+        if (IS_E ? (l0 >= 1) : (l0 <= th - 2)) {
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                const int l = a == 2 ? l0 + v : l0;
-                p0[v] = T(0);
-                p1[v] = T(0);
-                if ((unsigned)l >= (unsigned)th) continue;
-                if (sp) {
-                    p0[v] = sp[2 * v];
-                    p1[v] = sp[2 * v + 1];
-                } else {
-                    p0[v] = gp[2 * v];
-                    p1[v] = gp[2 * v + 1];
-                }
+                p0[v] = P::psi(p0[v], b, d[q0][v], cc);
+                p1[v] = P::psi(p1[v], b, d[q1][v], cc);
             }
-        }
+        } else {
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const int l = a == 2 ? l0 + v : l0;
-            if ((unsigned)l >= (unsigned)th) continue;
-            T b = bu, cc = cu;
-            if (a == 2) {
-                b = src.ctab ? src.ctab[g.coef_off[s] + l] : bt[l];
-                cc = src.ctab ? src.ctab[g.coef_off[s] + th + l] : ct[l];
-            }
-            if (IS_E ? (l >= 1) : (l <= th - 2)) {
-                const T d0 = a == 0 ? d[1][v] : (a == 1 ? d[2][v] : d[5][v]);
-                const T d1 = a == 0 ? d[0][v] : (a == 1 ? d[3][v] : d[4][v]);
-                p0[v] = P::psi(p0[v], b, d0, cc);
-                p1[v] = P::psi(p1[v], b, d1, cc);
-            } else {
+            for (int v = 0; v < V; ++v) {
                 p0[v] = P::mul(p0[v], b);
                 p1[v] = P::mul(p1[v], b);
             }
-            if (corr) {
-                // phi[(a+1)%3] = -p0, phi[(a+2)%3] = +p1 (fdtd/boundaries.py:457-459, 485-487);
-                // explicit branches keep the field values in registers
-                if (a == 0) {
-                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::cm(c, m[3 * v + 1]), -p0[v]);
-                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::cm(c, m[3 * v + 2]), p1[v]);
-                } else if (a == 1) {
-                    pml_correct<P, IS_E>(f[3 * v + 2], fl[3 * v + 2], P::cm(c, m[3 * v + 2]), -p0[v]);
-                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::cm(c, m[3 * v]), p1[v]);
-                } else {
-                    pml_correct<P, IS_E>(f[3 * v], fl[3 * v], P::cm(c, m[3 * v]), -p0[v]);
-                    pml_correct<P, IS_E>(f[3 * v + 1], fl[3 * v + 1], P::cm(c, m[3 * v + 1]), p1[v]);
-                }
+        }
+        if (corr) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                pml_correct<P, IS_E>(f[3 * v + c0], fl[3 * v + c0], P::cm(c, m[3 * v + c0]), -p0[v]);
+                pml_correct<P, IS_E>(f[3 * v + c1], fl[3 * v + c1], P::cm(c, m[3 * v + c1]), p1[v]);
             }
         }
         if (!store) {
-        } else if (V > 1 && a != 2) {
+        } else if constexpr (V > 1) {
             alignas(16) T pr[2 * V];
 #pragma unroll
             for (int v = 0; v < V; ++v) {
@@ -330,14 +309,77 @@ __device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, 
             }
             st_vec(gp, pr);
         } else {
+            gp[0] = p0[0];
+            gp[1] = p1[0];
+        }
+    } else {
+        // z slab: the V cells have consecutive slab-local indices, some may lie outside
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int l = l0 + v;
+            p0[v] = T(0);
+            p1[v] = T(0);
+            if ((unsigned)l >= (unsigned)th) continue;
+            if (sp) {
+                p0[v] = sp[2 * v];
+                p1[v] = sp[2 * v + 1];
+            } else {
+                p0[v] = gp[2 * v];
+                p1[v] = gp[2 * v + 1];
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int l = l0 + v;
+            if ((unsigned)l >= (unsigned)th) continue;
+            const T b = tb[l], cc = tc[l];
+            if (IS_E ? (l >= 1) : (l <= th - 2)) {
+                p0[v] = P::psi(p0[v], b, d[q0][v], cc);
+                p1[v] = P::psi(p1[v], b, d[q1][v], cc);
+            } else {
+                p0[v] = P::mul(p0[v], b);
+                p1[v] = P::mul(p1[v], b);
+            }
+            if (corr) {
+                pml_correct<P, IS_E>(f[3 * v + c0], fl[3 * v + c0], P::cm(c, m[3 * v + c0]), -p0[v]);
+                pml_correct<P, IS_E>(f[3 * v + c1], fl[3 * v + c1], P::cm(c, m[3 * v + c1]), p1[v]);
+            }
+        }
+        if (store) {
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                const int l = a == 2 ? l0 + v : l0;
+                const int l = l0 + v;
                 if ((unsigned)l >= (unsigned)th) continue;
                 gp[2 * v] = p0[v];
                 gp[2 * v + 1] = p1[v];
             }
         }
+    }
+}
+
+// PML auxiliaries and corrections of a thread's V cells, slab by slab in
+// boundary order (the per-cell order of fdtd/grid.py:279-291 is kept: every
+// slab touching a cell acts on it in ascending slab order).  d[q][v] are the
+// six one-sided differences of the neighbour field F of cell v, in the order
+// (dx F_y, dx F_z, dy F_x, dy F_z, dz F_x, dz F_y); a slab normal to axis a
+// drives its pair with (dF_(a+2)%3, dF_(a+1)%3) along a.  IS_E selects the E
+// rule (increment at slab-local index >= 1, E += c m phi) or the H rule
+// (index <= th-2, H -= c m phi).  store = false computes without writing the
+// updated auxiliaries (a neighbour's cell recomputed by the one-pass step);
+// HOFF selects the stage's H-side auxiliary slots (g.psi_offH/psi_pitchH) of
+// the one-pass step instead of g.psi_off/psi_pitch.  Each slab runs the code
+// compiled for its normal axis.
+template <class P, int V, bool IS_E, bool HOFF = false>
+__device__ __forceinline__ void apply_pml(const GridK &g, int i, int j, int k0, typename P::T c,
+                                          const typename P::T (&d)[6][V], const typename P::T (&m)[3 * V],
+                                          typename P::T (&f)[3 * V], typename P::T (&fl)[3 * V],
+                                          const PsiSrc<typename P::T> &src, unsigned slabs, bool store = true) {
+    for (unsigned sm = slabs; sm; sm &= sm - 1) {
+        const int s = __ffs(sm) - 1;
+        const int a = g.slab[s].axis;
+        if (a == 0) apply_pml_slab<P, V, IS_E, HOFF, 0>(g, s, i, j, k0, c, d, m, f, fl, src, store);
+        else if (a == 1) apply_pml_slab<P, V, IS_E, HOFF, 1>(g, s, i, j, k0, c, d, m, f, fl, src, store);
+        else apply_pml_slab<P, V, IS_E, HOFF, 2>(g, s, i, j, k0, c, d, m, f, fl, src, store);
     }
 }
 
