@@ -316,11 +316,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.epi_H = p.epi_E;
     }
     const int ks = p.pml_split ? kfs : g.nslab;  // slabs the fused pass handles
-    g.n_staged = g.n_direct = 0;
-    for (int s = 0; s < ks; ++s) {
+    g.n_staged = 0;
+    for (int s = 0; s < ks; ++s)
         if (!g.psi_direct || g.slab[s].axis == 2) g.staged_slab[g.n_staged++] = s;
-        else g.direct_slab[g.n_direct++] = s;
-    }
     // automatic choice: the TMA-staged kernels reach the HBM roofline on grids
     // without PML; with PML slabs the warps holding slab cells do more work per
     // plane and the staged kernels' per-plane CTA barrier makes the whole tile
@@ -1002,7 +1000,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             GridK &k = p.ko[dir];
             k = p.k;
             k.nslab_fused = k.nslab;
-            k.psi_direct = k.n_direct = 0;  // the one-pass stage holds every slab's auxiliary rows
+            k.psi_direct = 0;  // the one-pass stage holds every slab's auxiliary rows
             k.TZ = kl.TZ;
             k.TY = kl.TY;
             k.XC = kl.XC;

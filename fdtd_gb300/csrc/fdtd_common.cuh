@@ -71,8 +71,6 @@ struct GridK {
     int psi_direct;  // staged passes: auxiliaries of x/y slabs are read in-lane from global memory, not staged
     int n_staged;                  // staged passes: slabs whose auxiliary rows a stage holds,
     int staged_slab[kMaxSlabs];    // and their indices
-    int n_direct;                  // staged passes: fused slabs read in-lane (psi_direct), whose rows
-    int direct_slab[kMaxSlabs];    // the stage fill prefetches into L2, and their indices
     // one-pass step: offset and row pitch of each slab's H-side auxiliary slot
     int psi_offH[kMaxSlabs], psi_pitchH[kMaxSlabs];
     int coef_off[kMaxSlabs];  // per slab: offset (values) of its b/c tables in shared memory

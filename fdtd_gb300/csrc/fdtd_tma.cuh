@@ -78,11 +78,6 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uin
                  : "memory");
 }
 
-__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(src)), "r"(bytes)
-                 : "memory");
-}
-
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
@@ -175,30 +170,6 @@ __device__ __forceinline__ void fill_stage(const GridK &g, unsigned char *st, ui
         bytes[h] = nb;
         srcp[h] = psi + off;
         dst[h] = smem_u32(st + g.psi_off[s] + (size_t)rr * g.psi_pitch[s] * sizeof(T));
-    }
-    // auxiliary rows of slabs read in-lane: into L2 now, S-1 planes before the
-    // plane is computed (16-byte aligned rows of 2 * cells values, nz a
-    // multiple of the vector width)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int q = lane + 32 * h;
-        const int di = q / TY, rr = q % TY;
-        const int j = j0 + rr;
-        if (!with_psi || di >= g.n_direct || j >= g.ny) continue;
-        const SlabK &S = g.slab[g.direct_slab[di]];
-        const T *psi = (const T *)(is_E ? S.psiE_rd : S.psiH_rd);
-        const int cells = min(Zc, g.nz - k0c);
-        size_t off;
-        if (S.axis == 0) {
-            const int l = p - S.start;
-            if ((unsigned)l >= (unsigned)S.th) continue;
-            off = (((size_t)l * g.ny + j) * g.nz + k0c) * 2;
-        } else {
-            const int l = j - S.start;
-            if ((unsigned)l >= (unsigned)S.th) continue;
-            off = (((size_t)p * S.th + l) * g.nz + k0c) * 2;
-        }
-        bulk_prefetch_l2(psi + off, (uint32_t)(2 * cells * sizeof(T)));
     }
     const uint32_t tot = __reduce_add_sync(0xffffffffu, bytes[0] + bytes[1]);
     if (lane == 0) mbar_expect_tx(bar, field_tx + tot);
