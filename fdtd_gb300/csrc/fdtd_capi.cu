@@ -66,19 +66,30 @@ static bool box_ok(const int32_t lo[3], const int32_t hi[3], int nx, int ny, int
 // Ranges of CTA coordinates that a box touches, for the per-CTA lists.
 struct Tiling {
     int V, TZ, TY, XC, gz, gy, gx;
+    int o[3], e[3];  // the box of cells the tiles cover, [o, e) along x, y, z
 };
 
 // With `halo`, a CTA also covers the cell past its tile along each axis (the
 // one-pass step recomputes the new E there), so an item starting at a tile's
 // first cell is listed for the tile before it as well.
+// The tile ranges are inclusive, in tile coordinates of the tiling's box; an
+// item outside the box gets an empty range.
 static void cta_range(const Tiling &t, const int32_t lo[3], const int32_t hi[3], int r[6], bool halo = false) {
     const int zc = t.V * t.TZ, h = halo ? 1 : 0;
-    r[0] = std::max(0, lo[2] - h) / zc;
-    r[1] = (hi[2] - 1) / zc;
-    r[2] = std::max(0, lo[1] - h) / t.TY;
-    r[3] = (hi[1] - 1) / t.TY;
-    r[4] = std::max(0, lo[0] - h) / t.XC;
-    r[5] = (hi[0] - 1) / t.XC;
+    const int unit[3] = {t.XC, t.TY, zc};
+    for (int a = 0; a < 3; ++a) {
+        const int l = std::max(lo[a] - h, t.o[a]) - t.o[a], u = std::min(hi[a], t.e[a]) - t.o[a];
+        const int q = 2 * (2 - a);  // r: z range, y range, x range
+        if (u <= l) {
+            for (int k = 0; k < 6; k += 2) {
+                r[k] = 0;
+                r[k + 1] = -1;
+            }
+            return;
+        }
+        r[q] = l / unit[a];
+        r[q + 1] = (u - 1) / unit[a];
+    }
 }
 
 // CSR lists: for every CTA, the indices (into the device item array) of the
@@ -160,6 +171,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     g.nx = d->nx;
     g.ny = d->ny;
     g.nz = d->nz;
+    g.ex = d->nx;  // tiles cover the whole grid unless the plan partitions it
+    g.ey = d->ny;
+    g.ez = d->nz;
     g.courant = d->courant;
     g.courant_f = (float)d->courant;
     g.E = d->E;
@@ -253,11 +267,35 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                aligned16(d->inv_mu) && (!comp || (aligned16(d->E_lo) && aligned16(d->H_lo)));
     if (d->variant < 0 || d->variant > 2) return FDTD_ERR_ARGUMENT;
     if (d->variant == 2 && !vec) return FDTD_ERR_UNSUPPORTED;
-    if (d->pml_mode < 0 || d->pml_mode > 5) return FDTD_ERR_ARGUMENT;
-    // modes 4 and 5: modes 3 and 1 with the auxiliaries of x/y slabs read
-    // in-lane from global memory instead of staged through the ring
-    const int pml_base = d->pml_mode == 4 ? 3 : (d->pml_mode == 5 ? 1 : d->pml_mode);
-    g.psi_direct = d->pml_mode >= 4;
+    if (d->pml_mode < 0 || d->pml_mode > 4) return FDTD_ERR_ARGUMENT;
+    const int pml_base = d->pml_mode;
+    // Mode 4: interior/shell partition.  The box inside every PML slab (its
+    // z faces on 16-cell boundaries, so that the staged passes' tensor-map
+    // coordinates stay aligned) runs the slab-free staged pass; the rest of
+    // the grid, cut into up to six boxes, runs the register-streaming pass
+    // with every slab inside it.  Every cell is then read and written once
+    // per half step (the split slab kernels re-read each slab cell the bulk
+    // pass has just written), and each cell still gets bulk, objects, slabs
+    // in registration order and sources in that order, as in every mode.
+    int ibox[6] = {0, 0, 0, d->nx, d->ny, d->nz};  // tile box of the fused pass: [lo, hi) per axis
+    p.n_shell = 0;
+    if (pml_base == 4) {
+        int lo[3] = {0, 0, 0}, hi[3] = {d->nx, d->ny, d->nz};
+        for (int s = 0; s < g.nslab; ++s) {
+            const SlabK &S = g.slab[s];
+            if (S.high) hi[S.axis] = std::min(hi[S.axis], S.start);
+            else lo[S.axis] = std::max(lo[S.axis], S.start + S.th);
+        }
+        lo[2] = (lo[2] + 15) / 16 * 16;
+        hi[2] = hi[2] / vmax * vmax;
+        const bool inner = lo[0] < hi[0] && lo[1] < hi[1] && lo[2] < hi[2];
+        if (g.nslab == 0 || slab_after_periodic || !vec || !inner) return FDTD_ERR_UNSUPPORTED;
+        for (int a = 0; a < 3; ++a) {
+            ibox[a] = lo[a];
+            ibox[3 + a] = hi[a];
+        }
+        p.n_shell = -1;  // boxes cut below, once the interior tiling is known
+    }
     // PML slabs in kernels of their own let the fused pass run without slab
     // work (the staged kernels reach the HBM roofline there); the slab kernels
     // re-read only the slab cells.  The per-cell order of the reference is
@@ -281,7 +319,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     const long ncell = (long)d->nx * d->ny * d->nz;
     // 2D grids (nz = 1) of 8M cells and more split too (8192^2 float32: 63.1
     // vs 58.0 Gcell/s with 32-plane chunks)
-    p.pml_split = g.nslab > 0 &&
+    p.pml_split = g.nslab > 0 && pml_base != 4 &&
                   (pml_base >= 2 ||
                    (pml_base == 0 && ncell >= (8L << 20) &&
                     ((vec && (long)d->nz * 3 * (long)esize >= 768) || d->nz == 1)));
@@ -315,10 +353,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         }
         p.epi_H = p.epi_E;
     }
-    const int ks = p.pml_split ? kfs : g.nslab;  // slabs the fused pass handles
+    // extents of the fused pass's tile box
+    const int bnx = ibox[3] - ibox[0], bny = ibox[4] - ibox[1], bnz = ibox[5] - ibox[2];
+    // slabs the fused pass handles (none in the interior of a partition)
+    const int ks = p.n_shell ? 0 : (p.pml_split ? kfs : g.nslab);
     g.n_staged = 0;
-    for (int s = 0; s < ks; ++s)
-        if (!g.psi_direct || g.slab[s].axis == 2) g.staged_slab[g.n_staged++] = s;
+    for (int s = 0; s < ks; ++s) g.staged_slab[g.n_staged++] = s;
     // automatic choice: the TMA-staged kernels reach the HBM roofline on grids
     // without PML; with PML slabs the warps holding slab cells do more work per
     // plane and the staged kernels' per-plane CTA barrier makes the whole tile
@@ -326,8 +366,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     bool fused_z = false;  // a z slab inside the fused pass (divergent warps)
     for (int s = 0; s < ks; ++s) fused_z |= g.slab[s].axis == 2;
     const bool tma = d->variant == 2 ||
-                     (d->variant == 0 && vec && !fused_z && (long)d->nz * 3 * (long)esize >= 768);
+                     (d->variant == 0 && vec && !fused_z && (long)bnz * 3 * (long)esize >= 768);
     Tiling t{};
+    for (int a = 0; a < 3; ++a) {
+        t.o[a] = ibox[a];
+        t.e[a] = ibox[3 + a];
+    }
     int ctas_per_sm = 2;
     bool use_tma = tma;
     // staged passes: ring depth, stage bytes and auxiliary slot offsets of the E (0) and H (1) pass
@@ -358,7 +402,6 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             int slot_of[kMaxSlabs] = {0};
             for (int s = 0; s < ks; ++s) {
                 const SlabK &S = g.slab[s];
-                if (g.psi_direct && S.axis != 2) continue;  // read in-lane, no slot
                 const int unit = S.axis == 0 ? 1 : (S.axis == 1 ? TY : Zc);
                 const std::pair<int, int> rg(S.start / unit, (S.start + S.th - 1) / unit);
                 const int pitch = S.axis == 2 ? 2 * S.thp : 2 * Zc;
@@ -385,9 +428,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 sl.off = stage;
                 stage += (sl.bytes + 127) & ~(size_t)127;
             }
-            for (int s = 0; s < ks; ++s)
-                if (!g.psi_direct || g.slab[s].axis == 2)
-                    (off_out ? off_out : g.psi_off)[s] = (int)slots[slot_of[s]].off;
+            for (int s = 0; s < ks; ++s) (off_out ? off_out : g.psi_off)[s] = (int)slots[slot_of[s]].off;
             return stage;
         };
         int coef = 0;
@@ -418,8 +459,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         // drop (one-byte material indices): two CTAs per SM measured 77 vs
         // 67 Gcell/s on config 3 (float32) and 15.2 vs 12.6 (float64), and
         // the same as one CTA with full material arrays
-        int staged_slabs = 0;  // slabs whose auxiliary rows the stage holds
-        for (int s = 0; s < ks; ++s) staged_slabs += !g.psi_direct || g.slab[s].axis == 2;
+        const int staged_slabs = ks;  // slabs whose auxiliary rows the stage holds
         int rows = d->tile_rows;
         if (rows == 16 && staged_slabs > 4) {
             if (d->variant == 2) return FDTD_ERR_UNSUPPORTED;
@@ -427,8 +467,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         }
         if (rows == 0) {
             const long z32 = 32L * vmax, z16 = 16L * vmax;
-            const long waste32 = (d->nz + z32 - 1) / z32 * z32 - d->nz;
-            const long waste16 = (d->nz + z16 - 1) / z16 * z16 - d->nz;
+            const long waste32 = (bnz + z32 - 1) / z32 * z32 - bnz;
+            const long waste16 = (bnz + z16 - 1) / z16 * z16 - bnz;
             if (waste16 < waste32 && staged_slabs <= 4) {
                 rows = 16;
             } else {
@@ -486,15 +526,15 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     }
     if (!use_tma) {
         t.V = vec ? vmax : 1;
-        const int zthreads0 = (d->nz + t.V - 1) / t.V;
+        const int zthreads0 = (bnz + t.V - 1) / t.V;
         t.TZ = tile_width(zthreads0);
         t.TY = kThreads / t.TZ;
         g.stages = 0;
         p.variant = 1;
     }
-    const int zthreads = (d->nz + t.V - 1) / t.V;
+    const int zthreads = (bnz + t.V - 1) / t.V;
     t.gz = (zthreads + t.TZ - 1) / t.TZ;
-    t.gy = (d->ny + t.TY - 1) / t.TY;
+    t.gy = (bny + t.TY - 1) / t.TY;
     if (t.gy > 65535) return FDTD_ERR_UNSUPPORTED;
     if (d->x_chunk > 0) {
         t.XC = d->x_chunk;
@@ -510,13 +550,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         const long wave = (long)n_sm * ctas_per_sm;
         if (use_tma) {
             long chunks = cols >= 20L * wave ? 1 : (20L * wave + cols - 1) / cols;
-            chunks = std::max(1L, std::min(chunks, std::max(1L, (long)d->nx / 12)));
-            t.XC = (int)((d->nx + chunks - 1) / chunks);
+            chunks = std::max(1L, std::min(chunks, std::max(1L, (long)bnx / 12)));
+            t.XC = (int)((bnx + chunks - 1) / chunks);
         } else {
-            t.XC = register_chunk(d->nx, cols, wave);
+            t.XC = register_chunk(bnx, cols, wave);
         }
     }
-    t.gx = (d->nx + t.XC - 1) / t.XC;
+    t.gx = (bnx + t.XC - 1) / t.XC;
     if (t.gx > 65535) return FDTD_ERR_UNSUPPORTED;
     // adjoint kernels: register streaming, tiled like the register kernels
     {
@@ -670,6 +710,49 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     build_csr(t, items, srcE0, d->n_sources_E, se_off, se_idx);
     build_csr(t, items, srcH0, d->n_sources_H, sh_off, sh_idx);
 
+    // interior/shell partition: the boxes around the interior (x faces whole,
+    // y faces within the interior's x range, z faces within its x and y
+    // ranges), each tiled for the register-streaming kernels with its own
+    // per-CTA object and source lists
+    struct ShellBox {
+        Tiling t;
+        std::vector<int> lists[6];  // object, E source, H source lists (offsets, indices)
+        size_t at[6];
+    };
+    std::vector<ShellBox> shells;
+    if (p.n_shell) {
+        const int *lo = ibox, *hi = ibox + 3;
+        const int boxes[6][6] = {{0, 0, 0, lo[0], n[1], n[2]},         {hi[0], 0, 0, n[0], n[1], n[2]},
+                                 {lo[0], 0, 0, hi[0], lo[1], n[2]},     {lo[0], hi[1], 0, hi[0], n[1], n[2]},
+                                 {lo[0], lo[1], 0, hi[0], hi[1], lo[2]}, {lo[0], lo[1], hi[2], hi[0], hi[1], n[2]}};
+        for (const auto &b : boxes) {
+            if (b[3] <= b[0] || b[4] <= b[1] || b[5] <= b[2]) continue;
+            ShellBox sb;
+            Tiling &ts = sb.t;
+            for (int a = 0; a < 3; ++a) {
+                ts.o[a] = b[a];
+                ts.e[a] = b[3 + a];
+            }
+            ts.V = vmax;
+            const int zt = (b[5] - b[2]) / vmax;  // the z bounds are multiples of the vector width
+            ts.TZ = tile_width(zt);
+            ts.TY = kThreads / ts.TZ;
+            ts.gz = (zt + ts.TZ - 1) / ts.TZ;
+            ts.gy = (b[4] - b[1] + ts.TY - 1) / ts.TY;
+            ts.XC = register_chunk(b[3] - b[0], (long)ts.gz * ts.gy, 2L * n_sm);
+            ts.gx = (b[3] - b[0] + ts.XC - 1) / ts.XC;
+            if (ts.gy > 65535 || ts.gx > 65535) return FDTD_ERR_UNSUPPORTED;
+            build_csr(ts, items, 0, srcE0, sb.lists[0], sb.lists[1]);
+            build_csr(ts, items, srcE0, d->n_sources_E, sb.lists[2], sb.lists[3]);
+            build_csr(ts, items, srcH0, d->n_sources_H, sb.lists[4], sb.lists[5]);
+            shells.push_back(std::move(sb));
+        }
+        p.n_shell = (int)shells.size();
+    }
+    size_t shell_ints = 0;
+    for (const ShellBox &sb : shells)
+        for (const auto &v : sb.lists) shell_ints += v.size() + 1;
+
     // Launch order of the staged passes (and tile order of the persistent
     // loop over register-streaming tiles): the tiles that carry more work per
     // plane (object cells, weighted by the coefficient values they read, and
@@ -686,9 +769,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             for (int cx = r[4]; cx <= r[5]; ++cx)
                 for (int cy = r[2]; cy <= r[3]; ++cy)
                     for (int cz = r[0]; cz <= r[1]; ++cz) {
-                        const long ox = std::min(hi[0], (cx + 1) * t.XC) - std::max(lo[0], cx * t.XC);
-                        const long oy = std::min(hi[1], (cy + 1) * t.TY) - std::max(lo[1], cy * t.TY);
-                        const long oz = std::min(hi[2], (cz + 1) * zc) - std::max(lo[2], cz * zc);
+                        const int x0 = t.o[0] + cx * t.XC, y0 = t.o[1] + cy * t.TY, z0 = t.o[2] + cz * zc;
+                        const long ox = std::min({hi[0], x0 + t.XC, t.e[0]}) - std::max(lo[0], x0);
+                        const long oy = std::min({hi[1], y0 + t.TY, t.e[1]}) - std::max(lo[1], y0);
+                        const long oz = std::min({hi[2], z0 + zc, t.e[2]}) - std::max(lo[2], z0);
                         if (ox > 0 && oy > 0 && oz > 0) extra[cz + t.gz * (cy + (long)t.gy * cx)] += w * ox * oy * oz;
                     }
         };
@@ -723,6 +807,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     GridK kl;  // tiling and stage layout of the one-pass kernel
     memset(&kl, 0, sizeof(kl));
     Tiling to{};
+    for (int a = 0; a < 3; ++a) to.e[a] = n[a];
     std::vector<int> oo_off, oo_idx, ose_off, ose_idx, osh_off, osh_idx;
     {
         int why = 0;  // first reason the grid does not allow it (fdtd_plan_step_fusion)
@@ -918,7 +1003,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     const size_t b_lists = align(sizeof(int) * (obj_off.size() + obj_idx.size() + se_off.size() + se_idx.size() +
                                                 sh_off.size() + sh_idx.size() + oo_off.size() + oo_idx.size() +
                                                 ose_off.size() + ose_idx.size() + osh_off.size() + osh_idx.size() +
-                                                cta_order.size() + 13));
+                                                cta_order.size() + 13 + shell_ints));
     const size_t b_runs = align(sizeof(int2) * std::max<size_t>(1, runs.size()));
     const size_t b_status = 512;  // status word; at +256 the persistent loop's barrier and tile counters
     std::vector<char> host(b_items + b_lists + b_runs + b_status, 0);
@@ -946,6 +1031,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     put(osh_idx, at_osh_idx);
     size_t at_order;
     put(cta_order, at_order);
+    for (ShellBox &sb : shells)
+        for (int q = 0; q < 6; ++q) put(sb.lists[q], sb.at[q]);
     if (!runs.empty()) memcpy(host.data() + b_items + b_lists, runs.data(), sizeof(int2) * runs.size());
     ce = cudaMalloc(&p.dev_mem, host.size());
     if (ce != cudaSuccess) return cuda_fail(ce);
@@ -983,6 +1070,43 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.kf.nslab = p.fused_slabs;
         p.kf.nslab_fused = p.fused_slabs;
     }
+    for (int b = 0; b < p.n_shell; ++b) {
+        // a shell box: the register-streaming pass with every slab
+        GridK &k = p.kshell[b];
+        const ShellBox &sb = shells[b];
+        k = p.k;
+        k.ox = sb.t.o[0];
+        k.oy = sb.t.o[1];
+        k.oz = sb.t.o[2];
+        k.ex = sb.t.e[0];
+        k.ey = sb.t.e[1];
+        k.ez = sb.t.e[2];
+        k.TZ = sb.t.TZ;
+        k.TY = sb.t.TY;
+        k.XC = sb.t.XC;
+        k.obj_off = dl + sb.at[0];
+        k.obj_idx = dl + sb.at[1];
+        k.srcE_off = dl + sb.at[2];
+        k.srcE_idx = dl + sb.at[3];
+        k.srcH_off = dl + sb.at[4];
+        k.srcH_idx = dl + sb.at[5];
+        k.cta_order = nullptr;
+        k.n_staged = 0;
+        p.shell_grid[b] = dim3(sb.t.gz, sb.t.gy, sb.t.gx);
+        p.shell_block[b] = dim3(sb.t.TZ, sb.t.TY, 1);
+    }
+    if (p.n_shell) {
+        // the interior: no slab cells
+        p.kf.nslab = 0;
+        p.kf.nslab_fused = 0;
+        p.kf.n_staged = 0;
+        p.kf.ox = ibox[0];
+        p.kf.oy = ibox[1];
+        p.kf.oz = ibox[2];
+        p.kf.ex = ibox[3];
+        p.kf.ey = ibox[4];
+        p.kf.ez = ibox[5];
+    }
     p.kfH = p.kf;
     if (p.variant == 2) {
         GridK *pass_k[2] = {&p.kf, &p.kfH};
@@ -1000,7 +1124,6 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             GridK &k = p.ko[dir];
             k = p.k;
             k.nslab_fused = k.nslab;
-            k.psi_direct = 0;  // the one-pass stage holds every slab's auxiliary rows
             k.TZ = kl.TZ;
             k.TY = kl.TY;
             k.XC = kl.XC;
@@ -1060,7 +1183,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     {
         int coop = 0;
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        p.persist_ok = coop && p.variant == 1 && p.epi_E.empty() && p.epi_H.empty() && !p.has_feedback &&
+        p.persist_ok = coop && p.variant == 1 && p.n_shell == 0 && p.epi_E.empty() && p.epi_H.empty() && !p.has_feedback &&
                        p.n_current == 0 && (int)p.dft.size() <= kPersistMaxDft;
         // automatic: float32 below 3M cells, float64 below 8M (measured
         // against one launch per half step, register tiles, 500 steps: 64^3
@@ -1073,7 +1196,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     }
     p.stats_ctas = std::max(1, std::min(4 * n_sm, FDTD_STATS_STATIC_MAX_ROWS));
     p.device = dev;
-    p.launches_per_step = 2 + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
+    p.launches_per_step = 2 + 2 * p.n_shell + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
                           (p.n_current > 0 ? 1 : 0) + (int)p.dft.size();
     return FDTD_OK;
 }
@@ -1373,7 +1496,7 @@ int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8) {
     out8[3] = p.k.XC;
     out8[4] = (int64_t)p.grid.x * p.grid.y * p.grid.z;
     out8[5] = p.persistent ? 1 : p.launches_per_step;  // persistent: one launch per fdtd_run call
-    out8[6] = p.persistent ? 5 : p.variant + (p.pml_split ? 10 : 0);
+    out8[6] = p.persistent ? 5 : p.variant + (p.pml_split ? 10 : 0) + (p.n_shell ? 20 : 0);
     out8[7] = p.k.stages;
     return FDTD_OK;
 }

@@ -247,7 +247,7 @@ __device__ __forceinline__ void apply_pml_slab(const GridK &g, int s, int i, int
     else gofs = ((long)i * g.ny + j) * S.thp + l0;
     T *gp = psi + 2 * gofs;
     const T *sp = nullptr;
-    if (src.stage && (A == 2 || !g.psi_direct))
+    if (src.stage)
         sp = reinterpret_cast<const T *>(src.stage + (HOFF ? g.psi_offH[s] : g.psi_off[s])) +
              src.row * (HOFF ? g.psi_pitchH[s] : g.psi_pitch[s]) + (A == 2 ? 2 * l0 : 2 * (k0 - src.k0c));
     const T *tb = src.ctab ? src.ctab + g.coef_off[s] : bt;  // b at [l], c at [th + l] (shared) or ct[l]

@@ -62,13 +62,16 @@ struct GridK {
     const int *srcH_off, *srcH_idx;
     int fuse_src_E, fuse_src_H;      // sources applied inside the fused pass
     int TZ, TY, XC;                  // threads along z, rows along y, planes along x per CTA
+    // the box of cells the tiles cover: [ox, ex) x [oy, ey) x [oz, ez) (the
+    // whole grid, or one part of an interior/shell partition); oz is a
+    // multiple of 16 cells for the staged passes
+    int ox, oy, oz, ex, ey, ez;
     int stages;                      // shared-memory ring depth of the staged (TMA) kernels
     int *status;                     // device error word (bit 0: a pipeline wait timed out)
     // staged kernels: bytes of one stage, and per slab the byte offset (in a
     // stage) and row pitch (values) of its psi slot
     int stage_bytes;
     int psi_off[kMaxSlabs], psi_pitch[kMaxSlabs];
-    int psi_direct;  // staged passes: auxiliaries of x/y slabs are read in-lane from global memory, not staged
     int n_staged;                  // staged passes: slabs whose auxiliary rows a stage holds,
     int staged_slab[kMaxSlabs];    // and their indices
     // one-pass step: offset and row pitch of each slab's H-side auxiliary slot

@@ -32,11 +32,11 @@ __device__ __forceinline__ void tile_update_E(const GridK &g, const double *__re
     constexpr int N = 3 * V;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0 = (bx * g.TZ + tz) * V;
-    const int j = by * g.TY + ty;
-    const int xa = bz * g.XC;
-    const int xb = min(nx, xa + g.XC);
-    const bool act = (j < ny) && (k0 < nz);
+    const int k0 = g.oz + (bx * g.TZ + tz) * V;
+    const int j = g.oy + by * g.TY + ty;
+    const int xa = g.ox + bz * g.XC;
+    const int xb = min(g.ex, xa + g.XC);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const T c = courant_of<T>(g);
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
@@ -105,11 +105,11 @@ __device__ __forceinline__ void tile_update_H(const GridK &g, const double *__re
     constexpr int N = 3 * V;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0 = (bx * g.TZ + tz) * V;
-    const int j = by * g.TY + ty;
-    const int xa = bz * g.XC;
-    const int xb = min(nx, xa + g.XC);
-    const bool act = (j < ny) && (k0 < nz);
+    const int k0 = g.oz + (bx * g.TZ + tz) * V;
+    const int j = g.oy + by * g.TY + ty;
+    const int xa = g.ox + bz * g.XC;
+    const int xb = min(g.ex, xa + g.XC);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const T c = courant_of<T>(g);
     const T *__restrict__ E = (const T *)g.E;
     T *H = (T *)g.H;
@@ -149,7 +149,8 @@ __device__ __forceinline__ void tile_update_H(const GridK &g, const double *__re
         // (Ex, Ey) at k0+V: from the lane to the right, or from memory at a row end
         T kx = __shfl_down_sync(FULL_MASK, ec[0], 1);
         T ky = __shfl_down_sync(FULL_MASK, ec[1], 1);
-        if (tz == g.TZ - 1 && act && k0 + V < nz) {
+        // (the last lane of the tile, or the last of the box when the box ends inside the tile)
+        if ((tz == g.TZ - 1 || k0 + V >= g.ez) && act && k0 + V < nz) {
             kx = ld_field1<CG>(E + 3 * (cell0 + V));
             ky = ld_field1<CG>(E + 3 * (cell0 + V) + 1);
         }

@@ -71,6 +71,9 @@ static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) 
 }
 
 // Staged-kernel tile shapes (threads along z x rows): 32x8, 32x4, 16x16.
+// The fused pass of a half step: one launch over the tile box, then, for a
+// partitioned plan, one register-streaming launch per shell box (disjoint
+// cells; a half step writes only its own field, so their order is free).
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
@@ -78,14 +81,16 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
         if (p.kf.TY == 16) launch_tma<P, 16, 16>(p, is_E, wave, st);
         else if (p.kf.TY == 8) launch_tma<P, 32, 8>(p, is_E, wave, st);
         else launch_tma<P, 32, 4>(p, is_E, wave, st);
-        return;
-    }
-    if (p.V == 1) {
+    } else if (p.V == 1) {
         if (is_E) k_update_E<P, 1><<<p.grid, p.block, 0, st>>>(p.kf, wave);
         else k_update_H<P, 1><<<p.grid, p.block, 0, st>>>(p.kf, wave);
     } else {
         if (is_E) k_update_E<P, VV><<<p.grid, p.block, 0, st>>>(p.kf, wave);
         else k_update_H<P, VV><<<p.grid, p.block, 0, st>>>(p.kf, wave);
+    }
+    for (int b = 0; b < p.n_shell; ++b) {
+        if (is_E) k_update_E<P, VV><<<p.shell_grid[b], p.shell_block[b], 0, st>>>(p.kshell[b], wave);
+        else k_update_H<P, VV><<<p.shell_grid[b], p.shell_block[b], 0, st>>>(p.kshell[b], wave);
     }
 }
 

@@ -276,11 +276,11 @@ __global__ void __launch_bounds__(TZ *TY)
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const TileId tile = tile_of(g);
-    const int k0c = tile.bx * G::Zc, j0 = tile.by * TY;
+    const int k0c = g.oz + tile.bx * G::Zc, j0 = g.oy + tile.by * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
-    const int xa = tile.bz * g.XC, xb = min(nx, xa + g.XC);
+    const int xa = g.ox + tile.bz * g.XC, xb = min(g.ex, xa + g.XC);
     const int np = xb - xa;
-    const bool act = (j < ny) && (k0 < nz);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const int cta = tile.cta;
     const T c = courant_of<T>(g);
     const T *__restrict__ H = (const T *)g.H;
@@ -393,12 +393,12 @@ __global__ void __launch_bounds__(TZ *TY)
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const TileId tile = tile_of(g);
-    const int k0c = tile.bx * G::Zc, j0 = tile.by * TY;
+    const int k0c = g.oz + tile.bx * G::Zc, j0 = g.oy + tile.by * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
-    const int xa = tile.bz * g.XC, xb = min(nx, xa + g.XC);
+    const int xa = g.ox + tile.bz * g.XC, xb = min(g.ex, xa + g.XC);
     const int np = xb - xa;
     const int nfill = np + 1;  // E of plane xb is needed by the last plane
-    const bool act = (j < ny) && (k0 < nz);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const int cta = tile.cta;
     const T c = courant_of<T>(g);
     T *H = (T *)g.H;

@@ -214,16 +214,23 @@ TILINGS = [dict(variant=1, x_chunk=1), dict(variant=1, x_chunk=7), dict(variant=
            dict(variant=2, tile_rows=16, stages=2, pml_mode=2), dict(variant=2, tile_rows=16, stages=3, x_chunk=6,
                                                                  pml_mode=2),
            dict(variant=2, tile_rows=8, stages=3, pml_mode=3), dict(variant=1, pml_mode=3, x_chunk=5),
-           dict(variant=2, tile_rows=16, stages=2, pml_mode=3)]
+           dict(variant=2, tile_rows=16, stages=2, pml_mode=3),
+           dict(variant=2, tile_rows=8, pml_mode=4), dict(variant=2, tile_rows=16, stages=3, x_chunk=5, pml_mode=4),
+           dict(variant=2, tile_rows=4, stages=2, pml_mode=4), dict(variant=1, pml_mode=4, x_chunk=3)]
+
+# tiling()["pml_split"] of each PML mode: 1 slab kernels of their own, 2 interior/shell partition
+SPLIT_OF_MODE = {2: 1, 3: 1, 4: 2}
 
 
 @pytest.mark.parametrize("prec", ["float64", "float32", "float32c"])
 def test_kernel_variants_and_tiling_agree_bitwise(fd, prec):
     """Register-streaming and TMA-staged kernels, any tile shape and ring depth,
-    PML slabs inside the fused pass or in kernels of their own, give identical
-    bits (same per-cell arithmetic, only the data path differs).  Compensated
-    float32 renormalises its two-float pair after every slab kernel, so there
-    the separate-slab plans agree to round-off instead."""
+    PML slabs inside the fused pass, in kernels of their own, or in the
+    register-streaming pass over the shell boxes around a slab-free interior,
+    give identical bits (same per-cell arithmetic, only the data path
+    differs).  Compensated float32 renormalises its two-float pair after
+    every slab kernel, so there the separate-slab plans agree to round-off
+    instead."""
     fd.set_backend("gb300." + prec)
     build, _ = SCENES["c2_n24"]
     ref = build(fd)
@@ -234,9 +241,9 @@ def test_kernel_variants_and_tiling_agree_bitwise(fd, prec):
         g._ensure_engine().set_tuning(**tune)
         info = g._engine.tiling()
         assert info["variant"] == tune["variant"]
-        assert info["pml_split"] == (1 if tune.get("pml_mode", 1) >= 2 else 0)
+        assert info["pml_split"] == SPLIT_OF_MODE.get(tune.get("pml_mode", 1), 0)
         g.run(20, progress_bar=False)
-        if prec == "float32c" and tune.get("pml_mode", 1) >= 2:
+        if prec == "float32c" and tune.get("pml_mode", 1) in (2, 3):
             assert rel_l2(g.E, ref.E) <= 1e-6 and rel_l2(g.H, ref.H) <= 1e-6, tune
             continue
         assert torch.equal(g.E, ref.E) and torch.equal(g.H, ref.H), tune
@@ -244,12 +251,14 @@ def test_kernel_variants_and_tiling_agree_bitwise(fd, prec):
 
 
 @pytest.mark.parametrize("tile_rows", [8, 16])
-@pytest.mark.parametrize("pml_mode", [1, 2, 3])
+@pytest.mark.parametrize("pml_mode", [1, 2, 3, 4])
 @pytest.mark.parametrize("prec", ["float64", "float32"])
 def test_tma_variant_on_wide_grid_against_oracle(fd, prec, pml_mode, tile_rows):
     """A grid wider than one TMA tile along z and y (several CTAs, tile edges,
     periodic x, PML on y/z, objects crossing tile borders), PML slabs inside
-    the fused pass or in kernels of their own, 32x8 and 16x16 tiles."""
+    the fused pass, in kernels of their own, or in the shell boxes around a
+    slab-free interior (objects crossing the interior's faces), 32x8 and
+    16x16 tiles."""
     fd.set_backend("gb300." + prec)
     from fdtd_gb300 import scenes
 
@@ -261,7 +270,7 @@ def test_tma_variant_on_wide_grid_against_oracle(fd, prec, pml_mode, tile_rows):
         g[:, :, 0:5] = mod.PML()
         g[:, :, -4:] = mod.PML()
         g[0, :, :] = mod.PeriodicBoundary()
-        g[5:15, 6:30, 100:132] = mod.Object(permittivity=3.0)
+        g[5:15, 2:30, 100:134] = mod.Object(permittivity=3.0)
         g[3:12, 10:20, 60:70] = mod.AbsorbingObject(permittivity=2.0, conductivity=2e4)
         g[10, 18, 68] = mod.PointSource(period=13)
         g[:, 18, 60] = mod.LineDetector()
@@ -270,7 +279,7 @@ def test_tma_variant_on_wide_grid_against_oracle(fd, prec, pml_mode, tile_rows):
     g, o = build(fd), build(fo)
     g._ensure_engine().set_tuning(variant=2, pml_mode=pml_mode, tile_rows=tile_rows)
     assert g._engine.tiling()["variant"] == 2 and g._engine.tiling()["rows_y"] == tile_rows
-    assert g._engine.tiling()["pml_split"] == (1 if pml_mode >= 2 else 0)
+    assert g._engine.tiling()["pml_split"] == SPLIT_OF_MODE.get(pml_mode, 0)
     g.run(40, progress_bar=False)
     o.run(40)
     tol = TOL64 if prec == "float64" else TOL32
