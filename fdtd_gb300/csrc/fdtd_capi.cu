@@ -712,46 +712,74 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     // interior/shell partition: the boxes around the interior (x faces whole,
     // y faces within the interior's x range, z faces within its x and y
-    // ranges), each tiled for the register-streaming kernels with its own
-    // per-CTA object and source lists
-    struct ShellBox {
-        Tiling t;
-        std::vector<int> lists[6];  // object, E source, H source lists (offsets, indices)
-        size_t at[6];
-    };
-    std::vector<ShellBox> shells;
+    // ranges), one thread per cell, each block inside one box; per-block
+    // object and source lists
+    ShellK shk{};
+    std::vector<int> shl[6];  // object, E source, H source lists (offsets, indices)
     if (p.n_shell) {
         const int *lo = ibox, *hi = ibox + 3;
         const int boxes[6][6] = {{0, 0, 0, lo[0], n[1], n[2]},         {hi[0], 0, 0, n[0], n[1], n[2]},
                                  {lo[0], 0, 0, hi[0], lo[1], n[2]},     {lo[0], hi[1], 0, hi[0], n[1], n[2]},
                                  {lo[0], lo[1], 0, hi[0], hi[1], lo[2]}, {lo[0], lo[1], hi[2], hi[0], hi[1], n[2]}};
+        long blocks = 0;
         for (const auto &b : boxes) {
             if (b[3] <= b[0] || b[4] <= b[1] || b[5] <= b[2]) continue;
-            ShellBox sb;
-            Tiling &ts = sb.t;
+            const int q = shk.nbox++;
             for (int a = 0; a < 3; ++a) {
-                ts.o[a] = b[a];
-                ts.e[a] = b[3 + a];
+                shk.o[q][a] = b[a];
+                shk.n[q][a] = b[3 + a] - b[a];
             }
-            ts.V = vmax;
-            const int zt = (b[5] - b[2]) / vmax;  // the z bounds are multiples of the vector width
-            ts.TZ = tile_width(zt);
-            ts.TY = kThreads / ts.TZ;
-            ts.gz = (zt + ts.TZ - 1) / ts.TZ;
-            ts.gy = (b[4] - b[1] + ts.TY - 1) / ts.TY;
-            ts.XC = register_chunk(b[3] - b[0], (long)ts.gz * ts.gy, 2L * n_sm);
-            ts.gx = (b[3] - b[0] + ts.XC - 1) / ts.XC;
-            if (ts.gy > 65535 || ts.gx > 65535) return FDTD_ERR_UNSUPPORTED;
-            build_csr(ts, items, 0, srcE0, sb.lists[0], sb.lists[1]);
-            build_csr(ts, items, srcE0, d->n_sources_E, sb.lists[2], sb.lists[3]);
-            build_csr(ts, items, srcH0, d->n_sources_H, sb.lists[4], sb.lists[5]);
-            shells.push_back(std::move(sb));
+            shk.first[q] = (unsigned)blocks;
+            blocks += ((long)shk.n[q][0] * shk.n[q][1] * shk.n[q][2] + kThreads - 1) / kThreads;
+            if (blocks * kThreads >= (1L << 31)) return FDTD_ERR_UNSUPPORTED;
         }
-        p.n_shell = (int)shells.size();
+        shk.first[shk.nbox] = (unsigned)blocks;
+        // the blocks an item's cells fall in, ascending (rows of a box are
+        // consecutive runs of cells, boxes follow one another)
+        auto lists = [&](int first, int count, std::vector<int> &off, std::vector<int> &idx) {
+            off.assign(blocks + 1, 0);
+            for (int pass = 0; pass < 2; ++pass) {
+                std::vector<int> fill;
+                if (pass == 1) {
+                    for (long c = 0; c < blocks; ++c) off[c + 1] += off[c];
+                    idx.assign(off[blocks], 0);
+                    fill.assign(off.begin(), off.end() - 1);
+                }
+                for (int q = first; q < first + count; ++q) {
+                    const ItemK &it = items[q];
+                    long last = -1;
+                    for (int b = 0; b < shk.nbox; ++b) {
+                        int l[3], u[3];
+                        bool empty = false;
+                        for (int a = 0; a < 3; ++a) {
+                            l[a] = std::max(it.lo[a], shk.o[b][a]);
+                            u[a] = std::min(it.hi[a], shk.o[b][a] + shk.n[b][a]);
+                            empty |= u[a] <= l[a];
+                        }
+                        if (empty) continue;
+                        for (int x = l[0]; x < u[0]; ++x)
+                            for (int y = l[1]; y < u[1]; ++y) {
+                                const long row = ((long)(x - shk.o[b][0]) * shk.n[b][1] + (y - shk.o[b][1])) *
+                                                 shk.n[b][2];
+                                const long b0 = shk.first[b] + (row + l[2] - shk.o[b][2]) / kThreads;
+                                const long b1 = shk.first[b] + (row + u[2] - 1 - shk.o[b][2]) / kThreads;
+                                for (long blk = std::max(b0, last + 1); blk <= b1; ++blk) {
+                                    if (pass == 0) off[blk + 1]++;
+                                    else idx[fill[blk]++] = q;
+                                }
+                                last = std::max(last, b1);
+                            }
+                    }
+                }
+            }
+        };
+        lists(0, srcE0, shl[0], shl[1]);
+        lists(srcE0, d->n_sources_E, shl[2], shl[3]);
+        lists(srcH0, d->n_sources_H, shl[4], shl[5]);
+        p.n_shell = shk.nbox;
     }
     size_t shell_ints = 0;
-    for (const ShellBox &sb : shells)
-        for (const auto &v : sb.lists) shell_ints += v.size() + 1;
+    for (const auto &v : shl) shell_ints += v.size() + 1;
 
     // Launch order of the staged passes (and tile order of the persistent
     // loop over register-streaming tiles): the tiles that carry more work per
@@ -1031,8 +1059,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     put(osh_idx, at_osh_idx);
     size_t at_order;
     put(cta_order, at_order);
-    for (ShellBox &sb : shells)
-        for (int q = 0; q < 6; ++q) put(sb.lists[q], sb.at[q]);
+    size_t at_shell[6];
+    for (int q = 0; q < 6; ++q) put(shl[q], at_shell[q]);
     if (!runs.empty()) memcpy(host.data() + b_items + b_lists, runs.data(), sizeof(int2) * runs.size());
     ce = cudaMalloc(&p.dev_mem, host.size());
     if (ce != cudaSuccess) return cuda_fail(ce);
@@ -1070,30 +1098,18 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.kf.nslab = p.fused_slabs;
         p.kf.nslab_fused = p.fused_slabs;
     }
-    for (int b = 0; b < p.n_shell; ++b) {
-        // a shell box: the register-streaming pass with every slab
-        GridK &k = p.kshell[b];
-        const ShellBox &sb = shells[b];
+    if (p.n_shell) {
+        // the shell launch: every slab, its own per-block lists
+        GridK &k = p.kshell;
         k = p.k;
-        k.ox = sb.t.o[0];
-        k.oy = sb.t.o[1];
-        k.oz = sb.t.o[2];
-        k.ex = sb.t.e[0];
-        k.ey = sb.t.e[1];
-        k.ez = sb.t.e[2];
-        k.TZ = sb.t.TZ;
-        k.TY = sb.t.TY;
-        k.XC = sb.t.XC;
-        k.obj_off = dl + sb.at[0];
-        k.obj_idx = dl + sb.at[1];
-        k.srcE_off = dl + sb.at[2];
-        k.srcE_idx = dl + sb.at[3];
-        k.srcH_off = dl + sb.at[4];
-        k.srcH_idx = dl + sb.at[5];
+        k.obj_off = dl + at_shell[0];
+        k.obj_idx = dl + at_shell[1];
+        k.srcE_off = dl + at_shell[2];
+        k.srcE_idx = dl + at_shell[3];
+        k.srcH_off = dl + at_shell[4];
+        k.srcH_idx = dl + at_shell[5];
         k.cta_order = nullptr;
-        k.n_staged = 0;
-        p.shell_grid[b] = dim3(sb.t.gz, sb.t.gy, sb.t.gx);
-        p.shell_block[b] = dim3(sb.t.TZ, sb.t.TY, 1);
+        p.shellk = shk;
     }
     if (p.n_shell) {
         // the interior: no slab cells
@@ -1196,7 +1212,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     }
     p.stats_ctas = std::max(1, std::min(4 * n_sm, FDTD_STATS_STATIC_MAX_ROWS));
     p.device = dev;
-    p.launches_per_step = 2 + 2 * p.n_shell + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
+    p.launches_per_step = 2 + (p.n_shell ? 2 : 0) + (int)p.epi_E.size() + (int)p.epi_H.size() + (p.n_probe > 0 ? 2 : 0) +
                           (p.n_current > 0 ? 1 : 0) + (int)p.dft.size();
     return FDTD_OK;
 }

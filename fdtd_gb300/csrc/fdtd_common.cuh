@@ -90,6 +90,16 @@ struct GridK {
     const int *cta_order;  // staged passes: tile of each launched block, heaviest first (null: grid order)
 };
 
+// Shell boxes of an interior/shell partition, one thread per cell: box b
+// covers blocks [first[b], first[b + 1]) of the launch, its cells in
+// (x, y, z) order from origin o with extents n.  The GridK of the launch
+// carries per-block object and source lists.
+struct ShellK {
+    int nbox;
+    int o[6][3], n[6][3];
+    unsigned first[7];
+};
+
 template <class T>
 __device__ __forceinline__ T courant_of(const GridK &g);
 template <>

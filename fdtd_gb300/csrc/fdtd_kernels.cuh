@@ -172,6 +172,119 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
 }
 
 // ---------------------------------------------------------------------------
+// Shell boxes of an interior/shell partition: one thread per cell, the whole
+// per-cell half step (bulk, objects, every PML slab in order, sources) with
+// the neighbour values read through L1/L2, and the compact material copy
+// when the plan has one.  Each cell is read and written once; the slab-free
+// staged pass covers the interior.
+// ---------------------------------------------------------------------------
+
+// Cell of this thread: false past the end of its box.
+__device__ __forceinline__ bool shell_cell(const ShellK &sh, int &i, int &j, int &k) {
+    int b = 0;
+    while (b + 1 < sh.nbox && blockIdx.x >= sh.first[b + 1]) ++b;
+    const unsigned local = (blockIdx.x - sh.first[b]) * blockDim.x + threadIdx.x;
+    const unsigned nz = (unsigned)sh.n[b][2], ny = (unsigned)sh.n[b][1];
+    if (local >= (unsigned)sh.n[b][0] * ny * nz) return false;
+    const unsigned r = local / nz;
+    k = sh.o[b][2] + (int)(local - r * nz);
+    j = sh.o[b][1] + (int)(r % ny);
+    i = sh.o[b][0] + (int)(r / ny);
+    return true;
+}
+
+// Inverse material of one cell: the three values, a table row by index, or the one row.
+template <class T>
+__device__ __forceinline__ void shell_material(T (&m)[3], int mat, const T *full, const unsigned char *mid,
+                                               const T *lut, int nlut, size_t cell) {
+    if (mat == MAT_FULL) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) m[q] = full[3 * cell + q];
+    } else {
+        // an index past the table reads zeros, as in the staged passes
+        const int id = mat == MAT_IDS ? (int)mid[cell] : 0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) m[q] = id < nlut ? lut[3 * id + q] : T(0);
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const ShellK sh, const double *__restrict__ wave) {
+    using T = typename P::T;
+    int i, j, k;
+    if (!shell_cell(sh, i, j, k)) return;
+    const int ny = g.ny, nz = g.nz;
+    const size_t cell = ((size_t)i * ny + j) * nz + k;
+    const T *__restrict__ H = (const T *)g.H;
+    T *E = (T *)g.E;
+    T *Elo = (T *)g.Elo;
+    T hc[3], hp[3], hj[3], e[3], el[3], m[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        hc[q] = H[3 * cell + q];
+        hp[q] = i > 0 ? H[3 * (cell - (size_t)ny * nz) + q] : T(0);
+        hj[q] = j > 0 ? H[3 * (cell - nz) + q] : T(0);
+        e[q] = E[3 * cell + q];
+        el[q] = P::COMP ? Elo[3 * cell + q] : T(0);
+    }
+    const T kx = k > 0 ? H[3 * (cell - 1)] : T(0), ky = k > 0 ? H[3 * (cell - 1) + 1] : T(0);
+    shell_material<T>(m, g.mat_E, (const T *)g.ie, g.mid_E, (const T *)g.mlut_E, g.nlut_E, cell);
+    const int cta = blockIdx.x;
+    const int ob0 = g.obj_off[cta], ob1 = g.obj_off[cta + 1];
+    int sb0 = 0, sb1 = 0;
+    if (g.fuse_src_E) {
+        sb0 = g.srcE_off[cta];
+        sb1 = g.srcE_off[cta + 1];
+    }
+    const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned slabs = slab_mask_yz(g, j, k, 1) | slab_mask_x(g, i);
+    thread_E<P, 1>(g, wave, i, j, k, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
+                   slabs);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        E[3 * cell + q] = e[q];
+        if constexpr (P::COMP) Elo[3 * cell + q] = el[q];
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const ShellK sh, const double *__restrict__ wave) {
+    using T = typename P::T;
+    int i, j, k;
+    if (!shell_cell(sh, i, j, k)) return;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const size_t cell = ((size_t)i * ny + j) * nz + k;
+    const T *__restrict__ E = (const T *)g.E;
+    T *H = (T *)g.H;
+    T *Hlo = (T *)g.Hlo;
+    T ec[3], en[3], ej[3], h[3], hl[3], m[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        ec[q] = E[3 * cell + q];
+        en[q] = i + 1 < nx ? E[3 * (cell + (size_t)ny * nz) + q] : T(0);
+        ej[q] = j + 1 < ny ? E[3 * (cell + nz) + q] : T(0);
+        h[q] = H[3 * cell + q];
+        hl[q] = P::COMP ? Hlo[3 * cell + q] : T(0);
+    }
+    const T kx = k + 1 < nz ? E[3 * (cell + 1)] : T(0), ky = k + 1 < nz ? E[3 * (cell + 1) + 1] : T(0);
+    shell_material<T>(m, g.mat_H, (const T *)g.imu, g.mid_H, (const T *)g.mlut_H, g.nlut_H, cell);
+    const int cta = blockIdx.x;
+    int sb0 = 0, sb1 = 0;
+    if (g.fuse_src_H) {
+        sb0 = g.srcH_off[cta];
+        sb1 = g.srcH_off[cta + 1];
+    }
+    const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned slabs = slab_mask_yz(g, j, k, 1) | slab_mask_x(g, i);
+    thread_H<P, 1>(g, wave, i, j, k, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        H[3 * cell + q] = h[q];
+        if constexpr (P::COMP) Hlo[3 * cell + q] = hl[q];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Small kernels used when a periodic boundary fixes the order of the stages
 // after the fused pass, plus detectors, DFT, stand-alone curls and stats.
 // ---------------------------------------------------------------------------

@@ -72,8 +72,8 @@ static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) 
 
 // Staged-kernel tile shapes (threads along z x rows): 32x8, 32x4, 16x16.
 // The fused pass of a half step: one launch over the tile box, then, for a
-// partitioned plan, one register-streaming launch per shell box (disjoint
-// cells; a half step writes only its own field, so their order is free).
+// partitioned plan, one launch over the shell boxes (disjoint cells; a half
+// step writes only its own field, so their order is free).
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
@@ -88,9 +88,10 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
         if (is_E) k_update_E<P, VV><<<p.grid, p.block, 0, st>>>(p.kf, wave);
         else k_update_H<P, VV><<<p.grid, p.block, 0, st>>>(p.kf, wave);
     }
-    for (int b = 0; b < p.n_shell; ++b) {
-        if (is_E) k_update_E<P, VV><<<p.shell_grid[b], p.shell_block[b], 0, st>>>(p.kshell[b], wave);
-        else k_update_H<P, VV><<<p.shell_grid[b], p.shell_block[b], 0, st>>>(p.kshell[b], wave);
+    if (p.n_shell) {
+        const unsigned blocks = p.shellk.first[p.shellk.nbox];
+        if (is_E) k_shell_E<P><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
+        else k_shell_H<P><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
     }
 }
 

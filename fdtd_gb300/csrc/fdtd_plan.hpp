@@ -79,11 +79,11 @@ struct Plan {
     const int *persist_order;
     int persist_blocks;
     // interior/shell partition (pml_mode 4): the fused pass's tiles cover the
-    // interior box; n_shell boxes around it run the register-streaming
-    // kernels with every slab, each with its own tiling and per-CTA lists
+    // interior box; the n_shell boxes around it run one thread per cell with
+    // every slab (kshell: the plan's GridK with per-block lists)
     int n_shell;
-    GridK kshell[6];
-    dim3 shell_grid[6], shell_block[6];
+    GridK kshell;
+    ShellK shellk;
     GridK ko[2];
     CUtensorMap omaps[2][4];
     dim3 ogrid, oblock;
