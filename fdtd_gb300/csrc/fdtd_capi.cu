@@ -712,8 +712,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     // interior/shell partition: the boxes around the interior (x faces whole,
     // y faces within the interior's x range, z faces within its x and y
-    // ranges), one thread per cell, each block inside one box; per-block
-    // object and source lists
+    // ranges), one thread per vmax cells along z, each block inside one box;
+    // per-block object and source lists
     ShellK shk{};
     std::vector<int> shl[6];  // object, E source, H source lists (offsets, indices)
     if (p.n_shell) {
@@ -730,7 +730,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 shk.n[q][a] = b[3 + a] - b[a];
             }
             shk.first[q] = (unsigned)blocks;
-            blocks += ((long)shk.n[q][0] * shk.n[q][1] * shk.n[q][2] + kThreads - 1) / kThreads;
+            // vmax cells per thread along z
+            blocks += ((long)shk.n[q][0] * shk.n[q][1] * (shk.n[q][2] / vmax) + kThreads - 1) / kThreads;
             if (blocks * kThreads >= (1L << 31)) return FDTD_ERR_UNSUPPORTED;
         }
         shk.first[shk.nbox] = (unsigned)blocks;
@@ -759,10 +760,11 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                         if (empty) continue;
                         for (int x = l[0]; x < u[0]; ++x)
                             for (int y = l[1]; y < u[1]; ++y) {
+                                // thread slots of the row: vmax cells each
                                 const long row = ((long)(x - shk.o[b][0]) * shk.n[b][1] + (y - shk.o[b][1])) *
-                                                 shk.n[b][2];
-                                const long b0 = shk.first[b] + (row + l[2] - shk.o[b][2]) / kThreads;
-                                const long b1 = shk.first[b] + (row + u[2] - 1 - shk.o[b][2]) / kThreads;
+                                                 (shk.n[b][2] / vmax);
+                                const long b0 = shk.first[b] + (row + (l[2] - shk.o[b][2]) / vmax) / kThreads;
+                                const long b1 = shk.first[b] + (row + (u[2] - 1 - shk.o[b][2]) / vmax) / kThreads;
                                 for (long blk = std::max(b0, last + 1); blk <= b1; ++blk) {
                                     if (pass == 0) off[blk + 1]++;
                                     else idx[fill[blk]++] = q;

@@ -179,56 +179,64 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
 // staged pass covers the interior.
 // ---------------------------------------------------------------------------
 
-// Cell of this thread: false past the end of its box.
-__device__ __forceinline__ bool shell_cell(const ShellK &sh, int &i, int &j, int &k) {
+// The V cells (k0 .. k0+V-1 along z) of this thread: false past the end of
+// its box (box z extents and origins are multiples of V).
+template <int V>
+__device__ __forceinline__ bool shell_cells(const ShellK &sh, int &i, int &j, int &k0) {
     int b = 0;
     while (b + 1 < sh.nbox && blockIdx.x >= sh.first[b + 1]) ++b;
     const unsigned local = (blockIdx.x - sh.first[b]) * blockDim.x + threadIdx.x;
-    const unsigned nz = (unsigned)sh.n[b][2], ny = (unsigned)sh.n[b][1];
-    if (local >= (unsigned)sh.n[b][0] * ny * nz) return false;
-    const unsigned r = local / nz;
-    k = sh.o[b][2] + (int)(local - r * nz);
+    const unsigned nzv = (unsigned)(sh.n[b][2] / V), ny = (unsigned)sh.n[b][1];
+    if (local >= (unsigned)sh.n[b][0] * ny * nzv) return false;
+    const unsigned r = local / nzv;
+    k0 = sh.o[b][2] + V * (int)(local - r * nzv);
     j = sh.o[b][1] + (int)(r % ny);
     i = sh.o[b][0] + (int)(r / ny);
     return true;
 }
 
-// Inverse material of one cell: the three values, a table row by index, or the one row.
-template <class T>
-__device__ __forceinline__ void shell_material(T (&m)[3], int mat, const T *full, const unsigned char *mid,
-                                               const T *lut, int nlut, size_t cell) {
+// Inverse material of V cells: the values, table rows by index, or the one row.
+template <class T, int V>
+__device__ __forceinline__ void shell_material(T (&m)[3 * V], int mat, const T *full, const unsigned char *mid,
+                                               const T *lut, int nlut, size_t cell0) {
     if (mat == MAT_FULL) {
-#pragma unroll
-        for (int q = 0; q < 3; ++q) m[q] = full[3 * cell + q];
+        ld_vec_ro(m, full + 3 * cell0);
     } else {
-        // an index past the table reads zeros, as in the staged passes
-        const int id = mat == MAT_IDS ? (int)mid[cell] : 0;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) m[q] = id < nlut ? lut[3 * id + q] : T(0);
+        for (int v = 0; v < V; ++v) {
+            // an index past the table reads zeros, as in the staged passes
+            const int id = mat == MAT_IDS ? (int)mid[cell0 + v] : 0;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) m[3 * v + q] = id < nlut ? lut[3 * id + q] : T(0);
+        }
     }
 }
 
-template <class P>
+template <class P, int V>
 __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const ShellK sh, const double *__restrict__ wave) {
     using T = typename P::T;
-    int i, j, k;
-    if (!shell_cell(sh, i, j, k)) return;
+    constexpr int N = 3 * V;
+    int i, j, k0;
+    if (!shell_cells<V>(sh, i, j, k0)) return;
     const int ny = g.ny, nz = g.nz;
-    const size_t cell = ((size_t)i * ny + j) * nz + k;
+    const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
     T *Elo = (T *)g.Elo;
-    T hc[3], hp[3], hj[3], e[3], el[3], m[3];
+    alignas(16) T hc[N], hp[N], hj[N], e[N], el[N], m[N];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        hc[q] = H[3 * cell + q];
-        hp[q] = i > 0 ? H[3 * (cell - (size_t)ny * nz) + q] : T(0);
-        hj[q] = j > 0 ? H[3 * (cell - nz) + q] : T(0);
-        e[q] = E[3 * cell + q];
-        el[q] = P::COMP ? Elo[3 * cell + q] : T(0);
+    for (int q = 0; q < N; ++q) {
+        hp[q] = T(0);
+        hj[q] = T(0);
+        el[q] = T(0);
     }
-    const T kx = k > 0 ? H[3 * (cell - 1)] : T(0), ky = k > 0 ? H[3 * (cell - 1) + 1] : T(0);
-    shell_material<T>(m, g.mat_E, (const T *)g.ie, g.mid_E, (const T *)g.mlut_E, g.nlut_E, cell);
+    ld_vec_ro(hc, H + 3 * cell0);
+    if (i > 0) ld_vec_ro(hp, H + 3 * (cell0 - (size_t)ny * nz));
+    if (j > 0) ld_vec_ro(hj, H + 3 * (cell0 - nz));
+    ld_vec(e, E + 3 * cell0);
+    if constexpr (P::COMP) ld_vec(el, Elo + 3 * cell0);
+    const T kx = k0 > 0 ? H[3 * (cell0 - 1)] : T(0), ky = k0 > 0 ? H[3 * (cell0 - 1) + 1] : T(0);
+    shell_material<T, V>(m, g.mat_E, (const T *)g.ie, g.mid_E, (const T *)g.mlut_E, g.nlut_E, cell0);
     const int cta = blockIdx.x;
     const int ob0 = g.obj_off[cta], ob1 = g.obj_off[cta + 1];
     int sb0 = 0, sb1 = 0;
@@ -237,37 +245,39 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
         sb1 = g.srcE_off[cta + 1];
     }
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
-    const unsigned slabs = slab_mask_yz(g, j, k, 1) | slab_mask_x(g, i);
-    thread_E<P, 1>(g, wave, i, j, k, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
+    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
+    thread_E<P, V>(g, wave, i, j, k0, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
                    slabs);
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        E[3 * cell + q] = e[q];
-        if constexpr (P::COMP) Elo[3 * cell + q] = el[q];
-    }
+    st_vec(E + 3 * cell0, e);
+    if constexpr (P::COMP) st_vec(Elo + 3 * cell0, el);
 }
 
-template <class P>
+template <class P, int V>
 __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const ShellK sh, const double *__restrict__ wave) {
     using T = typename P::T;
-    int i, j, k;
-    if (!shell_cell(sh, i, j, k)) return;
+    constexpr int N = 3 * V;
+    int i, j, k0;
+    if (!shell_cells<V>(sh, i, j, k0)) return;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const size_t cell = ((size_t)i * ny + j) * nz + k;
+    const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
     const T *__restrict__ E = (const T *)g.E;
     T *H = (T *)g.H;
     T *Hlo = (T *)g.Hlo;
-    T ec[3], en[3], ej[3], h[3], hl[3], m[3];
+    alignas(16) T ec[N], en[N], ej[N], h[N], hl[N], m[N];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        ec[q] = E[3 * cell + q];
-        en[q] = i + 1 < nx ? E[3 * (cell + (size_t)ny * nz) + q] : T(0);
-        ej[q] = j + 1 < ny ? E[3 * (cell + nz) + q] : T(0);
-        h[q] = H[3 * cell + q];
-        hl[q] = P::COMP ? Hlo[3 * cell + q] : T(0);
+    for (int q = 0; q < N; ++q) {
+        en[q] = T(0);
+        ej[q] = T(0);
+        hl[q] = T(0);
     }
-    const T kx = k + 1 < nz ? E[3 * (cell + 1)] : T(0), ky = k + 1 < nz ? E[3 * (cell + 1) + 1] : T(0);
-    shell_material<T>(m, g.mat_H, (const T *)g.imu, g.mid_H, (const T *)g.mlut_H, g.nlut_H, cell);
+    ld_vec_ro(ec, E + 3 * cell0);
+    if (i + 1 < nx) ld_vec_ro(en, E + 3 * (cell0 + (size_t)ny * nz));
+    if (j + 1 < ny) ld_vec_ro(ej, E + 3 * (cell0 + nz));
+    ld_vec(h, H + 3 * cell0);
+    if constexpr (P::COMP) ld_vec(hl, Hlo + 3 * cell0);
+    const bool kn = k0 + V < nz;
+    const T kx = kn ? E[3 * (cell0 + V)] : T(0), ky = kn ? E[3 * (cell0 + V) + 1] : T(0);
+    shell_material<T, V>(m, g.mat_H, (const T *)g.imu, g.mid_H, (const T *)g.mlut_H, g.nlut_H, cell0);
     const int cta = blockIdx.x;
     int sb0 = 0, sb1 = 0;
     if (g.fuse_src_H) {
@@ -275,13 +285,10 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
         sb1 = g.srcH_off[cta + 1];
     }
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
-    const unsigned slabs = slab_mask_yz(g, j, k, 1) | slab_mask_x(g, i);
-    thread_H<P, 1>(g, wave, i, j, k, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        H[3 * cell + q] = h[q];
-        if constexpr (P::COMP) Hlo[3 * cell + q] = hl[q];
-    }
+    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
+    thread_H<P, V>(g, wave, i, j, k0, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
+    st_vec(H + 3 * cell0, h);
+    if constexpr (P::COMP) st_vec(Hlo + 3 * cell0, hl);
 }
 
 // ---------------------------------------------------------------------------

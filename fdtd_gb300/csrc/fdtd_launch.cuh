@@ -90,8 +90,8 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
     }
     if (p.n_shell) {
         const unsigned blocks = p.shellk.first[p.shellk.nbox];
-        if (is_E) k_shell_E<P><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
-        else k_shell_H<P><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
+        if (is_E) k_shell_E<P, VV><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
+        else k_shell_H<P, VV><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
     }
 }
 
