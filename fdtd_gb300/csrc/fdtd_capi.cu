@@ -712,7 +712,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     // interior/shell partition: the boxes around the interior (x faces whole,
     // y faces within the interior's x range, z faces within its x and y
-    // ranges), one thread per vmax cells along z, each block inside one box;
+    // ranges), one thread per kShellV cells along z, each block inside one box;
     // per-block object and source lists
     ShellK shk{};
     std::vector<int> shl[6];  // object, E source, H source lists (offsets, indices)
@@ -730,8 +730,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 shk.n[q][a] = b[3 + a] - b[a];
             }
             shk.first[q] = (unsigned)blocks;
-            // vmax cells per thread along z
-            blocks += ((long)shk.n[q][0] * shk.n[q][1] * (shk.n[q][2] / vmax) + kThreads - 1) / kThreads;
+            // kShellV cells per thread along z
+            blocks += ((long)shk.n[q][0] * shk.n[q][1] * (shk.n[q][2] / kShellV) + kThreads - 1) / kThreads;
             if (blocks * kThreads >= (1L << 31)) return FDTD_ERR_UNSUPPORTED;
         }
         shk.first[shk.nbox] = (unsigned)blocks;
@@ -760,11 +760,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                         if (empty) continue;
                         for (int x = l[0]; x < u[0]; ++x)
                             for (int y = l[1]; y < u[1]; ++y) {
-                                // thread slots of the row: vmax cells each
+                                // thread slots of the row: kShellV cells each
                                 const long row = ((long)(x - shk.o[b][0]) * shk.n[b][1] + (y - shk.o[b][1])) *
-                                                 (shk.n[b][2] / vmax);
-                                const long b0 = shk.first[b] + (row + (l[2] - shk.o[b][2]) / vmax) / kThreads;
-                                const long b1 = shk.first[b] + (row + (u[2] - 1 - shk.o[b][2]) / vmax) / kThreads;
+                                                 (shk.n[b][2] / kShellV);
+                                const long b0 = shk.first[b] + (row + (l[2] - shk.o[b][2]) / kShellV) / kThreads;
+                                const long b1 =
+                                    shk.first[b] + (row + (u[2] - 1 - shk.o[b][2]) / kShellV) / kThreads;
                                 for (long blk = std::max(b0, last + 1); blk <= b1; ++blk) {
                                     if (pass == 0) off[blk + 1]++;
                                     else idx[fill[blk]++] = q;
@@ -1112,6 +1113,10 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         k.srcH_idx = dl + at_shell[5];
         k.cta_order = nullptr;
         p.shellk = shk;
+        ce = cudaStreamCreateWithFlags(&p.shell_stream, cudaStreamNonBlocking);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p.shell_fork, cudaEventDisableTiming);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p.shell_join, cudaEventDisableTiming);
+        if (ce != cudaSuccess) return cuda_fail(ce);
     }
     if (p.n_shell) {
         // the interior: no slab cells
@@ -1230,8 +1235,11 @@ int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out) {
     *out = nullptr;
     fdtd_plan *h = new fdtd_plan();
     h->p.dev_mem = nullptr;
+    h->p.shell_stream = nullptr;
+    h->p.shell_fork = h->p.shell_join = nullptr;
     const int rc = create(desc, h->p);
     if (rc != FDTD_OK) {
+        release_shell(h->p);
         if (h->p.dev_mem) cudaFree(h->p.dev_mem);
         delete h;
         return rc;
@@ -1240,9 +1248,19 @@ int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out) {
     return FDTD_OK;
 }
 
+// The shell stream and its events (created with the plan's shell launch).
+static void release_shell(Plan &p) {
+    if (p.shell_fork) cudaEventDestroy(p.shell_fork);
+    if (p.shell_join) cudaEventDestroy(p.shell_join);
+    if (p.shell_stream) cudaStreamDestroy(p.shell_stream);
+    p.shell_fork = p.shell_join = nullptr;
+    p.shell_stream = nullptr;
+}
+
 int fdtd_plan_destroy(fdtd_plan *plan) {
     if (!plan) return FDTD_ERR_ARGUMENT;
     int rc = FDTD_OK;
+    release_shell(plan->p);
     if (plan->p.dev_mem) {
         cudaError_t e = cudaFree(plan->p.dev_mem);
         if (e != cudaSuccess) rc = cuda_fail(e);

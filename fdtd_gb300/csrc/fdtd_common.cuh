@@ -94,6 +94,10 @@ struct GridK {
 // covers blocks [first[b], first[b + 1]) of the launch, its cells in
 // (x, y, z) order from origin o with extents n.  The GridK of the launch
 // carries per-block object and source lists.
+// Cells per thread along z of the shell kernels (every precision): two keep
+// the registers low enough for four blocks of 256 threads per SM.
+constexpr int kShellV = 2;
+
 struct ShellK {
     int nbox;
     int o[6][3], n[6][3];

@@ -179,6 +179,41 @@ __global__ void __launch_bounds__(kThreads) k_update_H(const GridK g, const doub
 // staged pass covers the interior.
 // ---------------------------------------------------------------------------
 
+// Loads and stores of a thread's V cells: 16-byte accesses where the run's
+// size allows, else 8-byte ones (float pairs: a run of 3V floats starting at
+// an even cell is 8-byte aligned), else single values.
+template <bool RO, class T, int N>
+__device__ __forceinline__ void shell_ld(T (&dst)[N], const T *p) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        if constexpr (RO) ld_vec_ro(dst, p);
+        else ld_vec(dst, p);
+    } else if constexpr ((N * sizeof(T)) % 8 == 0) {
+        const uint2 *q = reinterpret_cast<const uint2 *>(p);
+#pragma unroll
+        for (int i = 0; i < (int)(N * sizeof(T) / 8); ++i) {
+            const uint2 t = RO ? __ldg(q + i) : q[i];
+            *reinterpret_cast<uint2 *>(&dst[i * 8 / sizeof(T)]) = t;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) dst[i] = RO ? __ldg(p + i) : p[i];
+    }
+}
+
+template <class T, int N>
+__device__ __forceinline__ void shell_st(T *p, const T (&src)[N]) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        st_vec(p, src);
+    } else if constexpr ((N * sizeof(T)) % 8 == 0) {
+        uint2 *q = reinterpret_cast<uint2 *>(p);
+#pragma unroll
+        for (int i = 0; i < (int)(N * sizeof(T) / 8); ++i) q[i] = *reinterpret_cast<const uint2 *>(&src[i * 8 / sizeof(T)]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = src[i];
+    }
+}
+
 // The V cells (k0 .. k0+V-1 along z) of this thread: false past the end of
 // its box (box z extents and origins are multiples of V).
 template <int V>
@@ -200,7 +235,7 @@ template <class T, int V>
 __device__ __forceinline__ void shell_material(T (&m)[3 * V], int mat, const T *full, const unsigned char *mid,
                                                const T *lut, int nlut, size_t cell0) {
     if (mat == MAT_FULL) {
-        ld_vec_ro(m, full + 3 * cell0);
+        shell_ld<true>(m, full + 3 * cell0);
     } else {
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -230,11 +265,11 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
         hj[q] = T(0);
         el[q] = T(0);
     }
-    ld_vec_ro(hc, H + 3 * cell0);
-    if (i > 0) ld_vec_ro(hp, H + 3 * (cell0 - (size_t)ny * nz));
-    if (j > 0) ld_vec_ro(hj, H + 3 * (cell0 - nz));
-    ld_vec(e, E + 3 * cell0);
-    if constexpr (P::COMP) ld_vec(el, Elo + 3 * cell0);
+    shell_ld<true>(hc, H + 3 * cell0);
+    if (i > 0) shell_ld<true>(hp, H + 3 * (cell0 - (size_t)ny * nz));
+    if (j > 0) shell_ld<true>(hj, H + 3 * (cell0 - nz));
+    shell_ld<false>(e, E + 3 * cell0);
+    if constexpr (P::COMP) shell_ld<false>(el, Elo + 3 * cell0);
     const T kx = k0 > 0 ? H[3 * (cell0 - 1)] : T(0), ky = k0 > 0 ? H[3 * (cell0 - 1) + 1] : T(0);
     shell_material<T, V>(m, g.mat_E, (const T *)g.ie, g.mid_E, (const T *)g.mlut_E, g.nlut_E, cell0);
     const int cta = blockIdx.x;
@@ -248,8 +283,8 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
     const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
     thread_E<P, V>(g, wave, i, j, k0, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
                    slabs);
-    st_vec(E + 3 * cell0, e);
-    if constexpr (P::COMP) st_vec(Elo + 3 * cell0, el);
+    shell_st(E + 3 * cell0, e);
+    if constexpr (P::COMP) shell_st(Elo + 3 * cell0, el);
 }
 
 template <class P, int V>
@@ -270,11 +305,11 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
         ej[q] = T(0);
         hl[q] = T(0);
     }
-    ld_vec_ro(ec, E + 3 * cell0);
-    if (i + 1 < nx) ld_vec_ro(en, E + 3 * (cell0 + (size_t)ny * nz));
-    if (j + 1 < ny) ld_vec_ro(ej, E + 3 * (cell0 + nz));
-    ld_vec(h, H + 3 * cell0);
-    if constexpr (P::COMP) ld_vec(hl, Hlo + 3 * cell0);
+    shell_ld<true>(ec, E + 3 * cell0);
+    if (i + 1 < nx) shell_ld<true>(en, E + 3 * (cell0 + (size_t)ny * nz));
+    if (j + 1 < ny) shell_ld<true>(ej, E + 3 * (cell0 + nz));
+    shell_ld<false>(h, H + 3 * cell0);
+    if constexpr (P::COMP) shell_ld<false>(hl, Hlo + 3 * cell0);
     const bool kn = k0 + V < nz;
     const T kx = kn ? E[3 * (cell0 + V)] : T(0), ky = kn ? E[3 * (cell0 + V) + 1] : T(0);
     shell_material<T, V>(m, g.mat_H, (const T *)g.imu, g.mid_H, (const T *)g.mlut_H, g.nlut_H, cell0);
@@ -287,8 +322,8 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
     const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
     thread_H<P, V>(g, wave, i, j, k0, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
-    st_vec(H + 3 * cell0, h);
-    if constexpr (P::COMP) st_vec(Hlo + 3 * cell0, hl);
+    shell_st(H + 3 * cell0, h);
+    if constexpr (P::COMP) shell_st(Hlo + 3 * cell0, hl);
 }
 
 // ---------------------------------------------------------------------------

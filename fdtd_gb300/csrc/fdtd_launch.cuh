@@ -71,12 +71,17 @@ static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) 
 }
 
 // Staged-kernel tile shapes (threads along z x rows): 32x8, 32x4, 16x16.
-// The fused pass of a half step: one launch over the tile box, then, for a
-// partitioned plan, one launch over the shell boxes (disjoint cells; a half
-// step writes only its own field, so their order is free).
+// The fused pass of a half step: one launch over the tile box and, for a
+// partitioned plan, one launch over the shell boxes on the plan's second
+// stream, joined before the half step's later stages (disjoint cells; a half
+// step writes only its own field, so the two may run at the same time).
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
+    if (p.n_shell) {
+        cudaEventRecord(p.shell_fork, st);
+        cudaStreamWaitEvent(p.shell_stream, p.shell_fork, 0);
+    }
     if (p.variant == 2) {
         if (p.kf.TY == 16) launch_tma<P, 16, 16>(p, is_E, wave, st);
         else if (p.kf.TY == 8) launch_tma<P, 32, 8>(p, is_E, wave, st);
@@ -90,8 +95,11 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
     }
     if (p.n_shell) {
         const unsigned blocks = p.shellk.first[p.shellk.nbox];
-        if (is_E) k_shell_E<P, VV><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
-        else k_shell_H<P, VV><<<blocks, kThreads, 0, st>>>(p.kshell, p.shellk, wave);
+        cudaStream_t ss = p.shell_stream;
+        if (is_E) k_shell_E<P, kShellV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
+        else k_shell_H<P, kShellV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
+        cudaEventRecord(p.shell_join, ss);
+        cudaStreamWaitEvent(st, p.shell_join, 0);
     }
 }
 

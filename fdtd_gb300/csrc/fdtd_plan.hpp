@@ -84,6 +84,10 @@ struct Plan {
     int n_shell;
     GridK kshell;
     ShellK shellk;
+    // the shell launch runs on a second stream beside the interior pass (it
+    // fills the interior pass's last wave); fork and join events
+    cudaStream_t shell_stream;
+    cudaEvent_t shell_fork, shell_join;
     GridK ko[2];
     CUtensorMap omaps[2][4];
     dim3 ogrid, oblock;
