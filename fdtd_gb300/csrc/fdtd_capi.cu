@@ -1228,6 +1228,15 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
 using namespace fdtd;
 
+// The shell stream and its events (created with the plan's shell launch).
+static void release_shell(Plan &p) {
+    if (p.shell_fork) cudaEventDestroy(p.shell_fork);
+    if (p.shell_join) cudaEventDestroy(p.shell_join);
+    if (p.shell_stream) cudaStreamDestroy(p.shell_stream);
+    p.shell_fork = p.shell_join = nullptr;
+    p.shell_stream = nullptr;
+}
+
 extern "C" {
 
 int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out) {
@@ -1246,15 +1255,6 @@ int fdtd_plan_create(const fdtd_grid_desc *desc, fdtd_plan **out) {
     }
     *out = h;
     return FDTD_OK;
-}
-
-// The shell stream and its events (created with the plan's shell launch).
-static void release_shell(Plan &p) {
-    if (p.shell_fork) cudaEventDestroy(p.shell_fork);
-    if (p.shell_join) cudaEventDestroy(p.shell_join);
-    if (p.shell_stream) cudaStreamDestroy(p.shell_stream);
-    p.shell_fork = p.shell_join = nullptr;
-    p.shell_stream = nullptr;
 }
 
 int fdtd_plan_destroy(fdtd_plan *plan) {
