@@ -712,7 +712,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
 
     // interior/shell partition: the boxes around the interior (x faces whole,
     // y faces within the interior's x range, z faces within its x and y
-    // ranges), one thread per kShellV cells along z, each block inside one box;
+    // ranges), one thread per sv cells along z, each block inside one box;
     // per-block object and source lists
     ShellK shk{};
     std::vector<int> shl[6];  // object, E source, H source lists (offsets, indices)
@@ -721,6 +721,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         const int boxes[6][6] = {{0, 0, 0, lo[0], n[1], n[2]},         {hi[0], 0, 0, n[0], n[1], n[2]},
                                  {lo[0], 0, 0, hi[0], lo[1], n[2]},     {lo[0], hi[1], 0, hi[0], n[1], n[2]},
                                  {lo[0], lo[1], 0, hi[0], hi[1], lo[2]}, {lo[0], lo[1], hi[2], hi[0], hi[1], n[2]}};
+        const int sv = d->precision == FDTD_FLOAT64 ? shell_v<double>() : shell_v<float>();
         long blocks = 0;
         for (const auto &b : boxes) {
             if (b[3] <= b[0] || b[4] <= b[1] || b[5] <= b[2]) continue;
@@ -730,8 +731,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 shk.n[q][a] = b[3 + a] - b[a];
             }
             shk.first[q] = (unsigned)blocks;
-            // kShellV cells per thread along z
-            blocks += ((long)shk.n[q][0] * shk.n[q][1] * (shk.n[q][2] / kShellV) + kThreads - 1) / kThreads;
+            blocks += ((long)shk.n[q][0] * shk.n[q][1] * (shk.n[q][2] / sv) + kThreads - 1) / kThreads;
             if (blocks * kThreads >= (1L << 31)) return FDTD_ERR_UNSUPPORTED;
         }
         shk.first[shk.nbox] = (unsigned)blocks;
@@ -760,12 +760,11 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                         if (empty) continue;
                         for (int x = l[0]; x < u[0]; ++x)
                             for (int y = l[1]; y < u[1]; ++y) {
-                                // thread slots of the row: kShellV cells each
+                                // thread slots of the row: sv cells each
                                 const long row = ((long)(x - shk.o[b][0]) * shk.n[b][1] + (y - shk.o[b][1])) *
-                                                 (shk.n[b][2] / kShellV);
-                                const long b0 = shk.first[b] + (row + (l[2] - shk.o[b][2]) / kShellV) / kThreads;
-                                const long b1 =
-                                    shk.first[b] + (row + (u[2] - 1 - shk.o[b][2]) / kShellV) / kThreads;
+                                                 (shk.n[b][2] / sv);
+                                const long b0 = shk.first[b] + (row + (l[2] - shk.o[b][2]) / sv) / kThreads;
+                                const long b1 = shk.first[b] + (row + (u[2] - 1 - shk.o[b][2]) / sv) / kThreads;
                                 for (long blk = std::max(b0, last + 1); blk <= b1; ++blk) {
                                     if (pass == 0) off[blk + 1]++;
                                     else idx[fill[blk]++] = q;

@@ -94,9 +94,12 @@ struct GridK {
 // covers blocks [first[b], first[b + 1]) of the launch, its cells in
 // (x, y, z) order from origin o with extents n.  The GridK of the launch
 // carries per-block object and source lists.
-// Cells per thread along z of the shell kernels (every precision): two keep
-// the registers low enough for four blocks of 256 threads per SM.
-constexpr int kShellV = 2;
+// Cells per thread along z of the shell kernels: two floats or one double,
+// which keeps the registers low enough for four blocks of 256 threads per SM.
+template <class T>
+constexpr int shell_v() {
+    return sizeof(T) == 4 ? 2 : 1;
+}
 
 struct ShellK {
     int nbox;

@@ -96,8 +96,9 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
     if (p.n_shell) {
         const unsigned blocks = p.shellk.first[p.shellk.nbox];
         cudaStream_t ss = p.shell_stream;
-        if (is_E) k_shell_E<P, kShellV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
-        else k_shell_H<P, kShellV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
+        constexpr int SV = shell_v<typename P::T>();
+        if (is_E) k_shell_E<P, SV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
+        else k_shell_H<P, SV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
         cudaEventRecord(p.shell_join, ss);
         cudaStreamWaitEvent(st, p.shell_join, 0);
     }
