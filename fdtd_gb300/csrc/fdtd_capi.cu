@@ -271,15 +271,22 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     const int pml_base = d->pml_mode;
     // Mode 4: interior/shell partition.  The box inside every PML slab (its
     // z faces on 16-cell boundaries, so that the staged passes' tensor-map
-    // coordinates stay aligned) runs the slab-free staged pass; the rest of
-    // the grid, cut into up to six boxes, runs the register-streaming pass
-    // with every slab inside it.  Every cell is then read and written once
-    // per half step (the split slab kernels re-read each slab cell the bulk
-    // pass has just written), and each cell still gets bulk, objects, slabs
-    // in registration order and sources in that order, as in every mode.
+    // coordinates stay aligned) runs the slab-free fused pass; the rest of
+    // the grid, cut into up to six boxes, runs one kernel with every slab
+    // (one thread per one or two cells).  Every cell is then read and
+    // written once per half step (the split slab kernels re-read each slab
+    // cell the bulk pass has just written), and each cell still gets bulk,
+    // objects, slabs in registration order and sources in that order, as in
+    // every mode.  Automatic on grids of 8M cells or more whose shell holds
+    // at least a fifth of the cells (float32 ms per step, split slabs vs
+    // partition: config 2 0.443 vs 0.375, config 5 0.618 vs 0.608; float64
+    // config 2 1.74 vs 1.49; float32c config 5 1.10 vs 0.85; config 3, 12 %
+    // of its cells in the shell, stays faster with its slabs split: 5.47 vs
+    // 5.77 float32).
     int ibox[6] = {0, 0, 0, d->nx, d->ny, d->nz};  // tile box of the fused pass: [lo, hi) per axis
     p.n_shell = 0;
-    if (pml_base == 4) {
+    const long ncell = (long)d->nx * d->ny * d->nz;
+    if (pml_base == 4 || pml_base == 0) {
         int lo[3] = {0, 0, 0}, hi[3] = {d->nx, d->ny, d->nz};
         for (int s = 0; s < g.nslab; ++s) {
             const SlabK &S = g.slab[s];
@@ -289,12 +296,20 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         lo[2] = (lo[2] + 15) / 16 * 16;
         hi[2] = hi[2] / vmax * vmax;
         const bool inner = lo[0] < hi[0] && lo[1] < hi[1] && lo[2] < hi[2];
-        if (g.nslab == 0 || slab_after_periodic || !vec || !inner) return FDTD_ERR_UNSUPPORTED;
-        for (int a = 0; a < 3; ++a) {
-            ibox[a] = lo[a];
-            ibox[3 + a] = hi[a];
+        const bool ok = g.nslab > 0 && !slab_after_periodic && vec && inner;
+        if (pml_base == 4 && !ok) return FDTD_ERR_UNSUPPORTED;
+        bool want = ok && pml_base == 4;
+        if (ok && pml_base == 0 && ncell >= (8L << 20)) {
+            const long inside = (long)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
+            want = 5 * (ncell - inside) >= ncell;
         }
-        p.n_shell = -1;  // boxes cut below, once the interior tiling is known
+        if (want) {
+            for (int a = 0; a < 3; ++a) {
+                ibox[a] = lo[a];
+                ibox[3 + a] = hi[a];
+            }
+            p.n_shell = -1;  // boxes cut below, once the interior tiling is known
+        }
     }
     // PML slabs in kernels of their own let the fused pass run without slab
     // work (the staged kernels reach the HBM roofline there); the slab kernels
@@ -316,10 +331,9 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // CTAs that hold them late, and their auxiliary rows enlarge every stage.
     // The automatic choice therefore keeps only leading y slabs, for float32
     // with compact materials.
-    const long ncell = (long)d->nx * d->ny * d->nz;
     // 2D grids (nz = 1) of 8M cells and more split too (8192^2 float32: 63.1
     // vs 58.0 Gcell/s with 32-plane chunks)
-    p.pml_split = g.nslab > 0 && pml_base != 4 &&
+    p.pml_split = g.nslab > 0 && p.n_shell == 0 &&
                   (pml_base >= 2 ||
                    (pml_base == 0 && ncell >= (8L << 20) &&
                     ((vec && (long)d->nz * 3 * (long)esize >= 768) || d->nz == 1)));
@@ -365,8 +379,14 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // wait for them, so the register-streaming kernels are faster there
     bool fused_z = false;  // a z slab inside the fused pass (divergent warps)
     for (int s = 0; s < ks; ++s) fused_z |= g.slab[s].axis == 2;
-    const bool tma = d->variant == 2 ||
-                     (d->variant == 0 && vec && !fused_z && (long)bnz * 3 * (long)esize >= 768);
+    // a partition's interior: the staged pass for float32 with compact
+    // materials on both passes, else the register-streaming one (measured:
+    // config 2, full permittivity, 0.375 vs 0.494 ms per step; config 5
+    // float64 2.49 vs 2.57, float32c 0.85 vs 0.95; float32 config 5 with
+    // compact materials 0.608 vs 0.636)
+    const bool shell_tma = d->precision == FDTD_FLOAT32 && mat_want[0] != MAT_FULL && mat_want[1] != MAT_FULL;
+    const bool tma = d->variant == 2 || (d->variant == 0 && vec && !fused_z && (long)bnz * 3 * (long)esize >= 768 &&
+                                         (p.n_shell == 0 || shell_tma));
     Tiling t{};
     for (int a = 0; a < 3; ++a) {
         t.o[a] = ibox[a];

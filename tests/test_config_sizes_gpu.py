@@ -101,16 +101,23 @@ def test_config1_full_size_float32(fd, c1_oracle, c1_fixture, prec, plan):
 
 
 # crops: builder, steps, full-size plan per precision, anisotropic (no bit identity)
+# the plans the full-size grids get: configs 2 and 5 the interior/shell
+# partition (register-streaming interior, or the staged one for float32 with
+# compact materials), config 3 its slabs in kernels of their own
 CROPS = {
     "c2_128": (lambda m: scenes.c2(m, n=128, pml=8), 8,
-               {"float64": dict(variant=2, pml_mode=2), "float32": dict(variant=2, pml_mode=2)}, False),
+               {"float64": dict(variant=1, pml_mode=4), "float32": dict(variant=1, pml_mode=4),
+                "float32c": dict(variant=1, pml_mode=4)}, False),
     "c3_192": (lambda m: scenes.c3(m, n=192, pml=5, detector=True), 8,
                {"float64": dict(variant=2, pml_mode=2, tile_rows=8),
-                "float32": dict(variant=2, pml_mode=3, tile_rows=8)}, False),
+                "float32": dict(variant=2, pml_mode=3, tile_rows=8),
+                "float32c": dict(variant=2, pml_mode=2, tile_rows=8)}, False),
     "c5_192x192x96": (lambda m: scenes.c5(m, nx=192, ny=192, nz=96, pml=10), 8,
-                      {"float64": dict(variant=2, pml_mode=2, tile_rows=16),
-                       "float32": dict(variant=2, pml_mode=2, tile_rows=16)}, True),
+                      {"float64": dict(variant=1, pml_mode=4),
+                       "float32": dict(variant=2, pml_mode=4, tile_rows=16),
+                       "float32c": dict(variant=1, pml_mode=4)}, True),
 }
+SPLIT_OF_MODE = {2: 1, 3: 1, 4: 2}
 
 
 def _random_start(shape, seed):
@@ -155,9 +162,10 @@ def test_config_crops_with_full_size_plans(fd, crop_oracle, name, prec):
     fd.set_backend("gb300." + prec)
     g = build(fd)
     eng = g._ensure_engine()
-    eng.set_tuning(**plans["float64" if prec == "float64" else "float32"])
+    eng.set_tuning(**plans[prec])
     info = eng.tiling()
-    assert info["variant"] == 2 and info["pml_split"] == 1, info
+    assert info["variant"] == plans[prec]["variant"], info
+    assert info["pml_split"] == SPLIT_OF_MODE[plans[prec]["pml_mode"]], info
     g.E.copy_(torch.as_tensor(E0, dtype=g.E.dtype))
     g.H.copy_(torch.as_tensor(H0, dtype=g.H.dtype))
     g.run(steps, progress_bar=False)
