@@ -285,6 +285,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // 5.77 float32).
     int ibox[6] = {0, 0, 0, d->nx, d->ny, d->nz};  // tile box of the fused pass: [lo, hi) per axis
     p.n_shell = 0;
+    p.shell_overlap = 0;
     const long ncell = (long)d->nx * d->ny * d->nz;
     if (pml_base == 4 || pml_base == 0) {
         int lo[3] = {0, 0, 0}, hi[3] = {d->nx, d->ny, d->nz};
@@ -1132,10 +1133,19 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         k.srcH_idx = dl + at_shell[5];
         k.cta_order = nullptr;
         p.shellk = shk;
-        ce = cudaStreamCreateWithFlags(&p.shell_stream, cudaStreamNonBlocking);
-        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p.shell_fork, cudaEventDisableTiming);
-        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p.shell_join, cudaEventDisableTiming);
-        if (ce != cudaSuccess) return cuda_fail(ce);
+        // beside a register-streaming interior in float32 and float32c the
+        // shell launch fills the interior's last wave (config 2 float32 0.375
+        // vs 0.395 ms per step, config 5 float32c 0.853 vs 0.870); the staged
+        // interior holds every register of its SMs and float64 is arithmetic
+        // bound, and both measured faster one after the other (config 5
+        // float32 0.578 vs 0.608, config 2 float64 1.39 vs 1.49)
+        p.shell_overlap = p.variant == 1 && d->precision != FDTD_FLOAT64;
+        if (p.shell_overlap) {
+            ce = cudaStreamCreateWithFlags(&p.shell_stream, cudaStreamNonBlocking);
+            if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p.shell_fork, cudaEventDisableTiming);
+            if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p.shell_join, cudaEventDisableTiming);
+            if (ce != cudaSuccess) return cuda_fail(ce);
+        }
     }
     if (p.n_shell) {
         // the interior: no slab cells

@@ -72,13 +72,14 @@ static void launch_tma(Plan &p, bool is_E, const double *wave, cudaStream_t st) 
 
 // Staged-kernel tile shapes (threads along z x rows): 32x8, 32x4, 16x16.
 // The fused pass of a half step: one launch over the tile box and, for a
-// partitioned plan, one launch over the shell boxes on the plan's second
-// stream, joined before the half step's later stages (disjoint cells; a half
-// step writes only its own field, so the two may run at the same time).
+// partitioned plan, one launch over the shell boxes, on the plan's second
+// stream (joined before the half step's later stages) when the plan lets the
+// two run at the same time (disjoint cells; a half step writes only its own
+// field).
 template <class P>
 static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st) {
     constexpr int VV = P::V;
-    if (p.n_shell) {
+    if (p.n_shell && p.shell_overlap) {
         cudaEventRecord(p.shell_fork, st);
         cudaStreamWaitEvent(p.shell_stream, p.shell_fork, 0);
     }
@@ -95,12 +96,14 @@ static void launch_fused(Plan &p, bool is_E, const double *wave, cudaStream_t st
     }
     if (p.n_shell) {
         const unsigned blocks = p.shellk.first[p.shellk.nbox];
-        cudaStream_t ss = p.shell_stream;
+        cudaStream_t ss = p.shell_overlap ? p.shell_stream : st;
         constexpr int SV = shell_v<typename P::T>();
         if (is_E) k_shell_E<P, SV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
         else k_shell_H<P, SV><<<blocks, kThreads, 0, ss>>>(p.kshell, p.shellk, wave);
-        cudaEventRecord(p.shell_join, ss);
-        cudaStreamWaitEvent(st, p.shell_join, 0);
+        if (p.shell_overlap) {
+            cudaEventRecord(p.shell_join, ss);
+            cudaStreamWaitEvent(st, p.shell_join, 0);
+        }
     }
 }
 

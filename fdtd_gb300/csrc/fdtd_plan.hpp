@@ -84,8 +84,9 @@ struct Plan {
     int n_shell;
     GridK kshell;
     ShellK shellk;
-    // the shell launch runs on a second stream beside the interior pass (it
-    // fills the interior pass's last wave); fork and join events
+    // shell_overlap: the shell launch runs on a second stream beside the
+    // interior pass; the stream, fork and join events
+    int shell_overlap;
     cudaStream_t shell_stream;
     cudaEvent_t shell_fork, shell_join;
     GridK ko[2];
