@@ -369,7 +369,8 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.epi_H = p.epi_E;
     }
     // extents of the fused pass's tile box
-    const int bnx = ibox[3] - ibox[0], bny = ibox[4] - ibox[1], bnz = ibox[5] - ibox[2];
+    const int bnx = ibox[3] - ibox[0], bny = ibox[4] - ibox[1];
+    int bnz = ibox[5] - ibox[2];
     // slabs the fused pass handles (none in the interior of a partition)
     const int ks = p.n_shell ? 0 : (p.pml_split ? kfs : g.nslab);
     g.n_staged = 0;
@@ -552,6 +553,17 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         t.TY = kThreads / t.TZ;
         g.stages = 0;
         p.variant = 1;
+    }
+    if (p.n_shell) {
+        // the interior's last z tile: when less than half of it would be
+        // active, its cells go to the shell (config 5: z 32..172 would take
+        // three 64-cell tiles, the last 12 cells active)
+        const int zc = t.V * t.TZ, rem = bnz % zc;
+        if (rem != 0 && 2 * rem < zc && bnz > zc) {
+            bnz -= rem;
+            ibox[5] -= rem;
+            t.e[2] = ibox[5];
+        }
     }
     const int zthreads = (bnz + t.V - 1) / t.V;
     t.gz = (zthreads + t.TZ - 1) / t.TZ;
