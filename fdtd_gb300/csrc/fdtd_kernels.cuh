@@ -258,8 +258,6 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
     T *Elo = (T *)g.Elo;
-    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
-    prefetch_pml<T, V, true>(g, i, j, k0, slabs);
     alignas(16) T hc[N], hp[N], hj[N], e[N], el[N], m[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
@@ -282,6 +280,7 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
         sb1 = g.srcE_off[cta + 1];
     }
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
     thread_E<P, V>(g, wave, i, j, k0, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
                    slabs);
     shell_st(E + 3 * cell0, e);
@@ -299,8 +298,6 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
     const T *__restrict__ E = (const T *)g.E;
     T *H = (T *)g.H;
     T *Hlo = (T *)g.Hlo;
-    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
-    prefetch_pml<T, V, false>(g, i, j, k0, slabs);
     alignas(16) T ec[N], en[N], ej[N], h[N], hl[N], m[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
@@ -323,6 +320,7 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
         sb1 = g.srcH_off[cta + 1];
     }
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
     thread_H<P, V>(g, wave, i, j, k0, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
     shell_st(H + 3 * cell0, h);
     if constexpr (P::COMP) shell_st(Hlo + 3 * cell0, hl);
