@@ -217,17 +217,8 @@ __device__ __forceinline__ void pml_correct(typename P::T &f, typename P::T &fl,
     else P::sub_prod(f, fl, cm, phi);
 }
 
-// PML auxiliaries and corrections of a thread's V cells, slab by slab in
-// boundary order (the per-cell order of fdtd/grid.py:279-291 is kept: every
-// slab touching a cell acts on it in ascending slab order).  d[q][v] are the
-// six one-sided differences of the neighbour field F of cell v, in the order
-// (dx F_y, dx F_z, dy F_x, dy F_z, dz F_x, dz F_y); a slab normal to axis a
-// drives its pair with (dF_(a+2)%3, dF_(a+1)%3) along a.  IS_E selects the E
-// rule (increment at slab-local index >= 1, E += c m phi) or the H rule
-// (index <= th-2, H -= c m phi).  store = false computes without writing the
-// updated auxiliaries (a neighbour's cell recomputed by the one-pass step);
-// HOFF selects the stage's H-side auxiliary slots (g.psi_offH/psi_pitchH) of
-// the one-pass step instead of g.psi_off/psi_pitch.
+// One PML slab (index s, normal to axis A) on a thread's V cells: the body
+// of apply_pml below, compiled once per normal axis.
 template <class P, int V, bool IS_E, bool HOFF, int A>
 __device__ __forceinline__ void apply_pml_slab(const GridK &g, int s, int i, int j, int k0, typename P::T c,
                                                const typename P::T (&d)[6][V], const typename P::T (&m)[3 * V],
