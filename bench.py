@@ -101,6 +101,10 @@ def parse():
                         "prints its own JSON line)")
     p.add_argument("--configs-only", action="store_true",
                    help="only configs 2 and 5 (prints its own JSON line)")
+    p.add_argument("--small", action="store_true",
+                   help="with --forward-only: the same scene generator on a smaller grid that gets the same "
+                        "automatic plan (config 2: 208^3 with a 13-cell PML; config 5: 256x256x192 with its 20-cell "
+                        "PML), about 1 GB on the device, for detailed ncu captures")
     return p.parse_args()
 
 
@@ -800,7 +804,10 @@ def main():
         from fdtd_gb300 import scenes
 
         fd.set_backend("gb300.float32")
-        g = scenes.c2(fd) if args.forward_only == "c2" else scenes.c5(fd)
+        if args.forward_only == "c2":
+            g = scenes.c2(fd, n=208, pml=13) if args.small else scenes.c2(fd)
+        else:
+            g = scenes.c5(fd, nx=256, ny=256) if args.small else scenes.c5(fd)
         g._ensure_engine().set_tuning(variant=args.variant, tile_rows=args.tile_rows, stages=args.stages,
                                       x_chunk=args.x_chunk, pml_mode=args.pml_mode, materials=args.materials,
                                       step_fusion=args.step_fusion)
