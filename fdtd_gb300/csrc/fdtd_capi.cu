@@ -763,7 +763,13 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
                 shk.o[q][a] = b[a];
                 shk.n[q][a] = b[3 + a] - b[a];
             }
+            for (int sl = 0; sl < g.nslab; ++sl) {
+                const SlabK &S = g.slab[sl];
+                if (S.start < b[3 + S.axis] && S.start + S.th > b[S.axis]) shk.slabs[q] |= 1u << sl;
+            }
             shk.first[q] = (unsigned)blocks;
+            magic_div((unsigned)(shk.n[q][2] / sv), shk.mz[q], shk.sz[q]);
+            magic_div((unsigned)shk.n[q][1], shk.my[q], shk.sy[q]);
             blocks += ((long)shk.n[q][0] * shk.n[q][1] * (shk.n[q][2] / sv) + kThreads - 1) / kThreads;
             if (blocks * kThreads >= (1L << 31)) return FDTD_ERR_UNSUPPORTED;
         }

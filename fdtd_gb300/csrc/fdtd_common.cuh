@@ -90,10 +90,10 @@ struct GridK {
     const int *cta_order;  // staged passes: tile of each launched block, heaviest first (null: grid order)
 };
 
-// Shell boxes of an interior/shell partition, one thread per cell: box b
-// covers blocks [first[b], first[b + 1]) of the launch, its cells in
-// (x, y, z) order from origin o with extents n.  The GridK of the launch
-// carries per-block object and source lists.
+// Shell boxes of an interior/shell partition: box b covers blocks
+// [first[b], first[b + 1]) of the launch, its cells in (x, y, z) order from
+// origin o with extents n, and meets the PML slabs in slabs[b].  The GridK
+// of the launch carries per-block object and source lists.
 // Cells per thread along z of the shell kernels: two floats or one double,
 // which keeps the registers low enough for four blocks of 256 threads per SM.
 template <class T>
@@ -105,7 +105,32 @@ struct ShellK {
     int nbox;
     int o[6][3], n[6][3];
     unsigned first[7];
+    unsigned slabs[6];  // per box: the PML slabs that reach into it
+    // per box: x / d as umulhi(x, m) >> sh for d = its thread slots per row
+    // (z) and its rows (y); exact for x < 2^31 (magic_div)
+    unsigned mz[6], my[6];
+    int sz[6], sy[6];
 };
+
+// Multiplier and shift of x / d for x < 2^31: with l = ceil(log2 d) and
+// m = ceil(2^(31+l) / d) < 2^32, floor(x m / 2^(31+l)) = floor(x / d), since
+// the error x (m - 2^(31+l)/d) / 2^(31+l) < 2^-l <= 1/d.  d = 1: m = 0, the
+// caller takes x itself.
+inline void magic_div(unsigned d, unsigned &m, int &shift) {
+    if (d <= 1) {
+        m = 0;
+        shift = 0;
+        return;
+    }
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    m = (unsigned)(((1ull << (31 + l)) + d - 1) / d);
+    shift = l - 1;
+}
+
+__device__ __forceinline__ unsigned div_magic(unsigned x, unsigned m, int shift) {
+    return m == 0 ? x : (__umulhi(x, m) >> shift);
+}
 
 template <class T>
 __device__ __forceinline__ T courant_of(const GridK &g);

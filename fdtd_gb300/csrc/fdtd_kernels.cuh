@@ -217,17 +217,34 @@ __device__ __forceinline__ void shell_st(T *p, const T (&src)[N]) {
 // The V cells (k0 .. k0+V-1 along z) of this thread: false past the end of
 // its box (box z extents and origins are multiples of V).
 template <int V>
-__device__ __forceinline__ bool shell_cells(const ShellK &sh, int &i, int &j, int &k0) {
+__device__ __forceinline__ bool shell_cells(const ShellK &sh, int &i, int &j, int &k0, unsigned &slabs) {
     int b = 0;
     while (b + 1 < sh.nbox && blockIdx.x >= sh.first[b + 1]) ++b;
     const unsigned local = (blockIdx.x - sh.first[b]) * blockDim.x + threadIdx.x;
     const unsigned nzv = (unsigned)(sh.n[b][2] / V), ny = (unsigned)sh.n[b][1];
     if (local >= (unsigned)sh.n[b][0] * ny * nzv) return false;
-    const unsigned r = local / nzv;
+    const unsigned r = div_magic(local, sh.mz[b], sh.sz[b]);
+    const unsigned x = div_magic(r, sh.my[b], sh.sy[b]);
     k0 = sh.o[b][2] + V * (int)(local - r * nzv);
-    j = sh.o[b][1] + (int)(r % ny);
-    i = sh.o[b][0] + (int)(r / ny);
+    j = sh.o[b][1] + (int)(r - x * ny);
+    i = sh.o[b][0] + (int)x;
+    slabs = sh.slabs[b];
     return true;
+}
+
+// The slabs among `cand` that contain cells of this thread (the slab mask of
+// the other kernels, tested only against the slabs that reach the box).
+template <int V>
+__device__ __forceinline__ unsigned shell_mask(const GridK &g, unsigned cand, int i, int j, int k0) {
+    unsigned m = 0;
+    for (unsigned sm = cand; sm; sm &= sm - 1) {
+        const int s = __ffs(sm) - 1;
+        const SlabK &S = g.slab[s];
+        const int c = S.axis == 0 ? i : (S.axis == 1 ? j : k0);
+        const int w = S.axis == 2 ? V : 1;
+        if (c < S.start + S.th && c + w > S.start) m |= 1u << s;
+    }
+    return m;
 }
 
 // Inverse material of V cells: the values, table rows by index, or the one row.
@@ -252,7 +269,8 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
     using T = typename P::T;
     constexpr int N = 3 * V;
     int i, j, k0;
-    if (!shell_cells<V>(sh, i, j, k0)) return;
+    unsigned cand;
+    if (!shell_cells<V>(sh, i, j, k0, cand)) return;
     const int ny = g.ny, nz = g.nz;
     const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
     const T *__restrict__ H = (const T *)g.H;
@@ -280,7 +298,7 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
         sb1 = g.srcE_off[cta + 1];
     }
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
-    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
+    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
     thread_E<P, V>(g, wave, i, j, k0, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
                    slabs);
     shell_st(E + 3 * cell0, e);
@@ -292,7 +310,8 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
     using T = typename P::T;
     constexpr int N = 3 * V;
     int i, j, k0;
-    if (!shell_cells<V>(sh, i, j, k0)) return;
+    unsigned cand;
+    if (!shell_cells<V>(sh, i, j, k0, cand)) return;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
     const T *__restrict__ E = (const T *)g.E;
@@ -320,7 +339,7 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
         sb1 = g.srcH_off[cta + 1];
     }
     const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
-    const unsigned slabs = slab_mask_yz(g, j, k0, V) | slab_mask_x(g, i);
+    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
     thread_H<P, V>(g, wave, i, j, k0, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
     shell_st(H + 3 * cell0, h);
     if constexpr (P::COMP) shell_st(Hlo + 3 * cell0, hl);
