@@ -157,6 +157,24 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
     // for the transposes: slab-free bulk passes, then one kernel per slab
     GridK gb = g;
     if (p.pml_split) gb.nslab = 0;
+    // partition plans: slab-free transposed passes over the interior box and
+    // the shell kernels with every slab around it
+    GridK gi = g;
+    if (p.n_shell) {
+        gi.nslab = 0;
+        gi.nslab_fused = 0;
+        gi.TZ = p.adjin_TZ;
+        gi.TY = p.adjin_TY;
+        gi.XC = p.adjin_XC;
+        gi.ox = p.kf.ox;
+        gi.oy = p.kf.oy;
+        gi.oz = p.kf.oz;
+        gi.ex = p.kf.ex;
+        gi.ey = p.kf.ey;
+        gi.ez = p.kf.ez;
+    }
+    constexpr int SV = shell_v<T>();
+    const unsigned shell_blocks = p.n_shell ? p.shellk.first[p.shellk.nbox] : 0u;
     // staged forward plans with the slabs on their own: staged transposed passes
     const bool staged = p.variant == 2 && p.pml_split && p.adj_V == (sizeof(T) == 4 ? 4 : 2);
     GridK gs = p.k;  // the forward staged tiling, launch order and material copies
@@ -205,6 +223,9 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
         if (staged) {
             const int rc = adj_staged<T>(p, gs, true, st);
             if (rc != FDTD_OK) return rc;
+        } else if (p.n_shell) {
+            k_adj_H<T, V><<<p.adjin_grid, p.adjin_block, 0, st>>>(gi, x);
+            k_adj_shell_H<T, SV><<<shell_blocks, kThreads, 0, st>>>(g, p.shellk, x);
         } else {
             k_adj_H<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
         }
@@ -245,6 +266,9 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
         if (staged) {
             const int rc = adj_staged<T>(p, gs, false, st);
             if (rc != FDTD_OK) return rc;
+        } else if (p.n_shell) {
+            k_adj_E<T, V><<<p.adjin_grid, p.adjin_block, 0, st>>>(gi, x);
+            k_adj_shell_E<T, SV><<<shell_blocks, kThreads, 0, st>>>(g, p.shellk, x);
         } else {
             k_adj_E<T, V><<<p.adj_grid, p.adj_block, 0, st>>>(gb, x);
         }

@@ -201,20 +201,74 @@ __device__ __forceinline__ void adj_pml_E(const GridK &g, const AdjAux &x, int i
     }
 }
 
+// Bulk of the transposed H half on a thread's V cells: lam_E (e) -=
+// curl_D1(w), w = c mu^-1 lam_H at the cells, wp / wj at plane i-1 / row
+// j-1, (kx, ky) = (w_x, w_y) at k0-1.
+template <class T, int V>
+__device__ __forceinline__ void adj_bulk_H(const GridK &g, int i, int j, int k0, const T (&w)[3 * V],
+                                           const T (&wp)[3 * V], const T (&wj)[3 * V], T kx, T ky, T (&e)[3 * V]) {
+    const bool xin = i < g.nx - 1, xbk = i > 0;
+    const bool yin = j < g.ny - 1, ybk = j > 0;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int k = k0 + v;
+        const bool zin = k < g.nz - 1, zbk = k > 0;
+        const T zx = v > 0 ? w[3 * (v - 1)] : kx;
+        const T zy = v > 0 ? w[3 * (v - 1) + 1] : ky;
+        const T wx = w[3 * v], wy = w[3 * v + 1], wz = w[3 * v + 2];
+        const T dy_z = (yin ? wz : T(0)) - (ybk ? wj[3 * v + 2] : T(0));
+        const T dz_y = (zin ? wy : T(0)) - (zbk ? zy : T(0));
+        const T dz_x = (zin ? wx : T(0)) - (zbk ? zx : T(0));
+        const T dx_z = (xin ? wz : T(0)) - (xbk ? wp[3 * v + 2] : T(0));
+        const T dx_y = (xin ? wy : T(0)) - (xbk ? wp[3 * v + 1] : T(0));
+        const T dy_x = (yin ? wx : T(0)) - (ybk ? wj[3 * v] : T(0));
+        e[3 * v] -= dy_z - dz_y;
+        e[3 * v + 1] -= dz_x - dx_z;
+        e[3 * v + 2] -= dx_y - dy_x;
+    }
+}
+
+// Bulk of the transposed E half on a thread's V cells: lam_H (h) +=
+// curl_D2(u), u = c eps^-1 lam_E at the cells, un / uj at plane i+1 / row
+// j+1, (kx, ky) = (u_x, u_y) at k0+V.
+template <class T, int V>
+__device__ __forceinline__ void adj_bulk_E(const GridK &g, int i, int j, int k0, const T (&u)[3 * V],
+                                           const T (&un)[3 * V], const T (&uj)[3 * V], T kx, T ky, T (&h)[3 * V]) {
+    const bool xn = i < g.nx - 1, xo = i > 0;
+    const bool yn = j < g.ny - 1, yo = j > 0;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int k = k0 + v;
+        const bool zn = k < g.nz - 1, zo = k > 0;
+        const T nzx = v < V - 1 ? u[3 * (v + 1)] : kx;
+        const T nzy = v < V - 1 ? u[3 * (v + 1) + 1] : ky;
+        const T ux = u[3 * v], uy = u[3 * v + 1], uz = u[3 * v + 2];
+        const T dy_z = (yn ? uj[3 * v + 2] : T(0)) - (yo ? uz : T(0));
+        const T dz_y = (zn ? nzy : T(0)) - (zo ? uy : T(0));
+        const T dz_x = (zn ? nzx : T(0)) - (zo ? ux : T(0));
+        const T dx_z = (xn ? un[3 * v + 2] : T(0)) - (xo ? uz : T(0));
+        const T dx_y = (xn ? un[3 * v + 1] : T(0)) - (xo ? uy : T(0));
+        const T dy_x = (yn ? uj[3 * v] : T(0)) - (yo ? ux : T(0));
+        h[3 * v] += dy_z - dz_y;
+        h[3 * v + 1] += dz_x - dx_z;
+        h[3 * v + 2] += dx_y - dy_x;
+    }
+}
+
 // Transposed H half: lam_E -= curl_D1(c mu^-1 lam_H) plus the H-side PML
 // terms.  g.E / g.H are lam_E / lam_H.  Same tiling and x-march as
 // k_update_E (the backward neighbours of w come from plane i-1, row j-1 and
-// the lane to the left).
+// the lane to the left), over the GridK's tile box.
 template <class T, int V>
 __global__ void __launch_bounds__(kThreads) k_adj_H(const GridK g, const AdjAux x) {
     constexpr int N = 3 * V;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0 = (blockIdx.x * g.TZ + tz) * V;
-    const int j = blockIdx.y * g.TY + ty;
-    const int xa = blockIdx.z * g.XC;
-    const int xb = min(nx, xa + g.XC);
-    const bool act = (j < ny) && (k0 < nz);
+    const int k0 = g.oz + (blockIdx.x * g.TZ + tz) * V;
+    const int j = g.oy + blockIdx.y * g.TY + ty;
+    const int xa = g.ox + blockIdx.z * g.XC;
+    const int xb = min(g.ex, xa + g.XC);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const T c = material_courant<T>(g);  // courant * material factor
     const T *LH = (const T *)g.H;
     T *LE = (T *)g.E;
@@ -244,25 +298,7 @@ __global__ void __launch_bounds__(kThreads) k_adj_H(const GridK g, const AdjAux 
             ky = (c * MU[3 * (cell0 - 1) + 1]) * LH[3 * (cell0 - 1) + 1];
         }
         if (act) {
-            const bool xin = i < nx - 1, xbk = i > 0;
-            const bool yin = j < ny - 1, ybk = j > 0;
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const int k = k0 + v;
-                const bool zin = k < nz - 1, zbk = k > 0;
-                const T zx = v > 0 ? w[3 * (v - 1)] : kx;
-                const T zy = v > 0 ? w[3 * (v - 1) + 1] : ky;
-                const T wx = w[3 * v], wy = w[3 * v + 1], wz = w[3 * v + 2];
-                const T dy_z = (yin ? wz : T(0)) - (ybk ? wj[3 * v + 2] : T(0));
-                const T dz_y = (zin ? wy : T(0)) - (zbk ? zy : T(0));
-                const T dz_x = (zin ? wx : T(0)) - (zbk ? zx : T(0));
-                const T dx_z = (xin ? wz : T(0)) - (xbk ? wp[3 * v + 2] : T(0));
-                const T dx_y = (xin ? wy : T(0)) - (xbk ? wp[3 * v + 1] : T(0));
-                const T dy_x = (yin ? wx : T(0)) - (ybk ? wj[3 * v] : T(0));
-                e[3 * v] -= dy_z - dz_y;
-                e[3 * v + 1] -= dz_x - dx_z;
-                e[3 * v + 2] -= dx_y - dy_x;
-            }
+            adj_bulk_H<T, V>(g, i, j, k0, w, wp, wj, kx, ky, e);
             const unsigned slabs = mask_yz | slab_mask_x(g, i);
             if (slabs) adj_pml_H<T, V>(g, x, i, j, k0, w, wp, wj, kx, ky, e, slabs);
             st_vec(LE + 3 * cell0, e);
@@ -281,11 +317,11 @@ __global__ void __launch_bounds__(kThreads) k_adj_E(const GridK g, const AdjAux 
     constexpr int N = 3 * V;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int k0 = (blockIdx.x * g.TZ + tz) * V;
-    const int j = blockIdx.y * g.TY + ty;
-    const int xa = blockIdx.z * g.XC;
-    const int xb = min(nx, xa + g.XC);
-    const bool act = (j < ny) && (k0 < nz);
+    const int k0 = g.oz + (blockIdx.x * g.TZ + tz) * V;
+    const int j = g.oy + blockIdx.y * g.TY + ty;
+    const int xa = g.ox + blockIdx.z * g.XC;
+    const int xb = min(g.ex, xa + g.XC);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const T c = material_courant<T>(g);  // courant * material factor
     const T *LE = (const T *)g.E;
     T *LH = (T *)g.H;
@@ -310,30 +346,12 @@ __global__ void __launch_bounds__(kThreads) k_adj_E(const GridK g, const AdjAux 
         // (u_x, u_y) at k0+V: from the lane to the right, or from memory at a row end
         T kx = __shfl_down_sync(FULL_MASK, u[0], 1);
         T ky = __shfl_down_sync(FULL_MASK, u[1], 1);
-        if (tz == g.TZ - 1 && act && k0 + V < nz) {
+        if ((tz == g.TZ - 1 || k0 + V >= g.ez) && act && k0 + V < nz) {
             kx = (c * IE[3 * (cell0 + V)]) * LE[3 * (cell0 + V)];
             ky = (c * IE[3 * (cell0 + V) + 1]) * LE[3 * (cell0 + V) + 1];
         }
         if (act) {
-            const bool xn = i < nx - 1, xo = i > 0;
-            const bool yn = j < ny - 1, yo = j > 0;
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const int k = k0 + v;
-                const bool zn = k < nz - 1, zo = k > 0;
-                const T nzx = v < V - 1 ? u[3 * (v + 1)] : kx;
-                const T nzy = v < V - 1 ? u[3 * (v + 1) + 1] : ky;
-                const T ux = u[3 * v], uy = u[3 * v + 1], uz = u[3 * v + 2];
-                const T dy_z = (yn ? uj[3 * v + 2] : T(0)) - (yo ? uz : T(0));
-                const T dz_y = (zn ? nzy : T(0)) - (zo ? uy : T(0));
-                const T dz_x = (zn ? nzx : T(0)) - (zo ? ux : T(0));
-                const T dx_z = (xn ? un[3 * v + 2] : T(0)) - (xo ? uz : T(0));
-                const T dx_y = (xn ? un[3 * v + 1] : T(0)) - (xo ? uy : T(0));
-                const T dy_x = (yn ? uj[3 * v] : T(0)) - (yo ? ux : T(0));
-                h[3 * v] += dy_z - dz_y;
-                h[3 * v + 1] += dz_x - dx_z;
-                h[3 * v + 2] += dx_y - dy_x;
-            }
+            adj_bulk_E<T, V>(g, i, j, k0, u, un, uj, kx, ky, h);
             const unsigned slabs = mask_yz | slab_mask_x(g, i);
             if (slabs) adj_pml_E<T, V>(g, x, i, j, k0, u, un, uj, kx, ky, h, slabs);
             st_vec(LH + 3 * cell0, h);
@@ -341,6 +359,81 @@ __global__ void __launch_bounds__(kThreads) k_adj_E(const GridK g, const AdjAux 
 #pragma unroll
         for (int q = 0; q < N; ++q) u[q] = un[q];
     }
+}
+
+// Shell boxes of an interior/shell partition plan, transposed: one thread per
+// V cells along z, the bulk and every PML slab's terms of the transposed half
+// (the same per-cell arithmetic as k_adj_H / k_adj_E), neighbours read
+// through L1/L2.  The slab-free k_adj_H / k_adj_E cover the interior box.
+
+// dst[q] = (c * m[q]) * lam[q] for the 3V values at cell0 (8- or 16-byte loads).
+template <class T, int V>
+__device__ __forceinline__ void shell_scaled(T (&dst)[3 * V], const T *lam, const T *m, size_t cell0, T c) {
+    alignas(16) T l[3 * V], mm[3 * V];
+    shell_ld<false>(l, lam + 3 * cell0);
+    shell_ld<true>(mm, m + 3 * cell0);
+#pragma unroll
+    for (int q = 0; q < 3 * V; ++q) dst[q] = (c * mm[q]) * l[q];
+}
+
+template <class T, int V>
+__global__ void __launch_bounds__(kThreads) k_adj_shell_H(const GridK g, const ShellK sh, const AdjAux x) {
+    constexpr int N = 3 * V;
+    int i, j, k0;
+    unsigned cand;
+    if (!shell_cells<V>(sh, i, j, k0, cand)) return;
+    const int ny = g.ny, nz = g.nz;
+    const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
+    const T c = material_courant<T>(g);
+    const T *LH = (const T *)g.H;
+    T *LE = (T *)g.E;
+    const T *MU = (const T *)g.imu;
+    alignas(16) T w[N], wp[N], wj[N], e[N];
+    zero(wp);
+    zero(wj);
+    shell_scaled<T, V>(w, LH, MU, cell0, c);
+    if (i > 0) shell_scaled<T, V>(wp, LH, MU, cell0 - (size_t)ny * nz, c);
+    if (j > 0) shell_scaled<T, V>(wj, LH, MU, cell0 - nz, c);
+    shell_ld<false>(e, LE + 3 * cell0);
+    T kx = T(0), ky = T(0);
+    if (k0 > 0) {
+        kx = (c * MU[3 * (cell0 - 1)]) * LH[3 * (cell0 - 1)];
+        ky = (c * MU[3 * (cell0 - 1) + 1]) * LH[3 * (cell0 - 1) + 1];
+    }
+    adj_bulk_H<T, V>(g, i, j, k0, w, wp, wj, kx, ky, e);
+    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
+    if (slabs) adj_pml_H<T, V>(g, x, i, j, k0, w, wp, wj, kx, ky, e, slabs);
+    shell_st(LE + 3 * cell0, e);
+}
+
+template <class T, int V>
+__global__ void __launch_bounds__(kThreads) k_adj_shell_E(const GridK g, const ShellK sh, const AdjAux x) {
+    constexpr int N = 3 * V;
+    int i, j, k0;
+    unsigned cand;
+    if (!shell_cells<V>(sh, i, j, k0, cand)) return;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const size_t cell0 = ((size_t)i * ny + j) * nz + k0;
+    const T c = material_courant<T>(g);
+    const T *LE = (const T *)g.E;
+    T *LH = (T *)g.H;
+    const T *IE = (const T *)g.ie;
+    alignas(16) T u[N], un[N], uj[N], h[N];
+    zero(un);
+    zero(uj);
+    shell_scaled<T, V>(u, LE, IE, cell0, c);
+    if (i + 1 < nx) shell_scaled<T, V>(un, LE, IE, cell0 + (size_t)ny * nz, c);
+    if (j + 1 < ny) shell_scaled<T, V>(uj, LE, IE, cell0 + nz, c);
+    shell_ld<false>(h, LH + 3 * cell0);
+    T kx = T(0), ky = T(0);
+    if (k0 + V < nz) {
+        kx = (c * IE[3 * (cell0 + V)]) * LE[3 * (cell0 + V)];
+        ky = (c * IE[3 * (cell0 + V) + 1]) * LE[3 * (cell0 + V) + 1];
+    }
+    adj_bulk_E<T, V>(g, i, j, k0, u, un, uj, kx, ky, h);
+    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
+    if (slabs) adj_pml_E<T, V>(g, x, i, j, k0, u, un, uj, kx, ky, h, slabs);
+    shell_st(LH + 3 * cell0, h);
 }
 
 // PML transposes of one slab on their own (plans whose forward pass runs the

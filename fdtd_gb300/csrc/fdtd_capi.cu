@@ -606,6 +606,17 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.adj_XC = XC;
         p.adj_grid = dim3(gz, gy, (d->nx + XC - 1) / XC);
         p.adj_block = dim3(TZ, TY, 1);
+        if (p.n_shell) {
+            // the interior box of a partition (its z bounds are multiples of V)
+            const int zti = bnz / V, TZi = tile_width(zti), TYi = kThreads / TZi;
+            const int gzi = (zti + TZi - 1) / TZi, gyi = (bny + TYi - 1) / TYi;
+            const int XCi = register_chunk(bnx, (long)gzi * gyi, 2L * n_sm);
+            p.adjin_TZ = TZi;
+            p.adjin_TY = TYi;
+            p.adjin_XC = XCi;
+            p.adjin_grid = dim3(gzi, gyi, (bnx + XCi - 1) / XCi);
+            p.adjin_block = dim3(TZi, TYi, 1);
+        }
     }
     p.V = t.V;
     g.TZ = t.TZ;

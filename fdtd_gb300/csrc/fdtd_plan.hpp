@@ -59,6 +59,9 @@ struct Plan {
     int adj_V;
     dim3 adj_grid, adj_block;
     int adj_TZ, adj_TY, adj_XC;
+    // partition plans: the transposed passes' tiling of the interior box
+    dim3 adjin_grid, adjin_block;
+    int adjin_TZ, adjin_TY, adjin_XC;
     std::vector<ItemK> items_host;
     int n_objects, srcE0, n_srcE, srcH0, n_srcH;
     int slab_boundary[kMaxSlabs];
