@@ -175,13 +175,24 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
     }
     constexpr int SV = shell_v<T>();
     const unsigned shell_blocks = p.n_shell ? p.shellk.first[p.shellk.nbox] : 0u;
-    // staged forward plans with the slabs on their own: staged transposed passes
-    const bool staged = p.variant == 2 && p.pml_split && p.adj_V == (sizeof(T) == 4 ? 4 : 2);
+    // staged forward plans with the slabs on their own, or staged partition
+    // interiors: staged transposed passes (over the interior box, then the
+    // shell kernels)
+    const bool staged = p.variant == 2 && (p.pml_split || p.n_shell) && p.adj_V == (sizeof(T) == 4 ? 4 : 2);
     GridK gs = p.k;  // the forward staged tiling, launch order and material copies
     gs.E = a->lam_E;
     gs.H = a->lam_H;
     gs.Elo = gs.Hlo = nullptr;
     gs.nslab = 0;
+    gs.nslab_fused = 0;
+    if (p.n_shell) {
+        gs.ox = p.kf.ox;
+        gs.oy = p.kf.oy;
+        gs.oz = p.kf.oz;
+        gs.ex = p.kf.ex;
+        gs.ey = p.kf.ey;
+        gs.ez = p.kf.ez;
+    }
     auto slab_cells = [&](const SlabK &S) {
         return (long)(S.axis == 0 ? S.th : g.nx) * (S.axis == 1 ? S.th : g.ny) * (S.axis == 2 ? S.th : g.nz);
     };
@@ -223,6 +234,7 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
         if (staged) {
             const int rc = adj_staged<T>(p, gs, true, st);
             if (rc != FDTD_OK) return rc;
+            if (p.n_shell) k_adj_shell_H<T, SV><<<shell_blocks, kThreads, 0, st>>>(g, p.shellk, x);
         } else if (p.n_shell) {
             k_adj_H<T, V><<<p.adjin_grid, p.adjin_block, 0, st>>>(gi, x);
             k_adj_shell_H<T, SV><<<shell_blocks, kThreads, 0, st>>>(g, p.shellk, x);
@@ -266,6 +278,7 @@ static int adjoint_impl(Plan &p, const fdtd_adjoint_args *a, cudaStream_t st) {
         if (staged) {
             const int rc = adj_staged<T>(p, gs, false, st);
             if (rc != FDTD_OK) return rc;
+            if (p.n_shell) k_adj_shell_E<T, SV><<<shell_blocks, kThreads, 0, st>>>(g, p.shellk, x);
         } else if (p.n_shell) {
             k_adj_E<T, V><<<p.adjin_grid, p.adjin_block, 0, st>>>(gi, x);
             k_adj_shell_E<T, SV><<<shell_blocks, kThreads, 0, st>>>(g, p.shellk, x);

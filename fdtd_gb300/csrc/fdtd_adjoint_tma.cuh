@@ -95,11 +95,11 @@ __global__ void __launch_bounds__(TZ *TY)
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const TileId tile = tile_of(g);
-    const int k0c = tile.bx * G::Zc, j0 = tile.by * TY;
+    const int k0c = g.oz + tile.bx * G::Zc, j0 = g.oy + tile.by * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
-    const int xa = tile.bz * g.XC, xb = min(nx, xa + g.XC);
+    const int xa = g.ox + tile.bz * g.XC, xb = min(g.ex, xa + g.XC);
     const int np = xb - xa;
-    const bool act = (j < ny) && (k0 < nz);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const T c = material_courant<T>(g);
     T *LE = (T *)g.E;
     const T *LH = (const T *)g.H;
@@ -208,12 +208,12 @@ __global__ void __launch_bounds__(TZ *TY)
     const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * TZ + tz;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const TileId tile = tile_of(g);
-    const int k0c = tile.bx * G::Zc, j0 = tile.by * TY;
+    const int k0c = g.oz + tile.bx * G::Zc, j0 = g.oy + tile.by * TY;
     const int k0 = k0c + tz * V, j = j0 + ty;
-    const int xa = tile.bz * g.XC, xb = min(nx, xa + g.XC);
+    const int xa = g.ox + tile.bz * g.XC, xb = min(g.ex, xa + g.XC);
     const int np = xb - xa;
     const int nfill = np + 1;  // lam_E of plane xb is needed by the last plane
-    const bool act = (j < ny) && (k0 < nz);
+    const bool act = (j < g.ey) && (k0 < g.ez);
     const T c = material_courant<T>(g);
     T *LH = (T *)g.H;
     const int xN = 3 * k0c * (int)sizeof(T) / 8;
