@@ -301,7 +301,9 @@ class Engine:
         the TMA tile rows (4 or 8 with 32-thread-wide tiles, 16 with 16-wide) and
         ring stages, where the PML slabs run
         (0 auto, 1 inside the fused pass, 2 kernels of their own; 3 only the
-        leading x/y slabs split off), how the staged passes read the
+        leading x/y slabs split off; 4 interior/shell partition: the fused
+        pass over the box inside every slab, one kernel with every slab over
+        the shell around it), how the staged passes read the
         materials (0 a one-byte index into a table of distinct value triples,
         or nothing for a uniform material, where the materials allow; 1 the
         full arrays), and whether full steps run as one pass each (0 auto:
@@ -326,6 +328,8 @@ class Engine:
         keys = ("cells_per_thread_z", "threads_z", "rows_y", "planes_x", "ctas", "launches_per_step",
                 "variant", "stages")
         info = dict(zip(keys, (int(v) for v in out)))
+        # pml_split: 0 slabs inside the fused pass, 1 slabs in kernels of
+        # their own, 2 interior/shell partition (the interior's tiling reported)
         info["pml_split"] = info["variant"] // 10
         info["variant"] %= 10
         # 5: the persistent loop over register-streaming tiles

@@ -140,7 +140,12 @@ typedef struct {
     int32_t pml_mode;     /* PML slabs: 0 automatic, 1 inside the fused pass, 2 one kernel per
                              slab after the fused pass (auxiliary update and correction),
                              3 the slabs normal to x or y that lead the boundary list inside
-                             the fused pass and the others in kernels of their own */
+                             the fused pass and the others in kernels of their own,
+                             4 interior/shell partition: the fused pass (staged or register
+                             streaming) over the box inside every slab, one kernel with every
+                             slab over the boxes around it (needs nz a multiple of the vector
+                             width, every PML before any periodic boundary and a non-empty
+                             interior; else FDTD_ERR_UNSUPPORTED) */
     double courant;
     void *E;              /* [nx][ny][nz][3] */
     void *H;
@@ -376,9 +381,10 @@ int fdtd_plan_step_fusion(const fdtd_plan *plan, int32_t *allowed, int32_t *acti
 /* Launch tiling chosen by the plan: out[0..7] = cells per thread along z,
  * threads along z, rows along y, planes along x per CTA, CTAs, kernels per
  * full step, variant (1 register streaming, 2 TMA-staged; plus 10 when the
- * PML slabs run in kernels of their own; 4 one pass per full step, whose
- * tiling is then reported; 5 the persistent loop of register-streaming
- * tiles, one launch per fdtd_run call), ring stages. */
+ * PML slabs run in kernels of their own, plus 20 for an interior/shell
+ * partition, whose interior tiling is then reported; 4 one pass per full
+ * step, whose tiling is then reported; 5 the persistent loop of
+ * register-streaming tiles, one launch per fdtd_run call), ring stages. */
 int fdtd_plan_tiling(const fdtd_plan *plan, int64_t *out8);
 
 const char *fdtd_status_string(int32_t status);
