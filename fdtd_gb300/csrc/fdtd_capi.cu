@@ -294,7 +294,15 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
             if (S.high) hi[S.axis] = std::min(hi[S.axis], S.start);
             else lo[S.axis] = std::max(lo[S.axis], S.start + S.th);
         }
-        lo[2] = (lo[2] + 15) / 16 * 16;
+        // z faces: on 16-cell boundaries where a staged interior reads a
+        // one-byte material index map (its tensor-map x coordinate is in
+        // bytes), else on vector-width boundaries (the field maps' x
+        // coordinate, 3 k esize / 8, is then even); the staged interior is
+        // the automatic one for float32 with compact materials
+        const bool stg = d->variant == 2 || (d->variant == 0 && d->precision == FDTD_FLOAT32 &&
+                                              mat_want[0] != MAT_FULL && mat_want[1] != MAT_FULL);
+        const int za = stg && (mat_want[0] == MAT_IDS || mat_want[1] == MAT_IDS) ? 16 : vmax;
+        lo[2] = (lo[2] + za - 1) / za * za;
         hi[2] = hi[2] / vmax * vmax;
         const bool inner = lo[0] < hi[0] && lo[1] < hi[1] && lo[2] < hi[2];
         const bool ok = g.nslab > 0 && !slab_after_periodic && vec && inner;
@@ -555,11 +563,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         p.variant = 1;
     }
     if (p.n_shell) {
-        // the interior's last z tile: when less than half of it would be
+        // a staged interior's last z tile: when less than half of it would be
         // active, its cells go to the shell (config 5: z 32..172 would take
-        // three 64-cell tiles, the last 12 cells active)
+        // three 64-cell tiles, the last 12 cells active; the tile's loads
+        // cover all of it, a register-streaming tile's idle lanes load nothing)
         const int zc = t.V * t.TZ, rem = bnz % zc;
-        if (rem != 0 && 2 * rem < zc && bnz > zc) {
+        if (use_tma && rem != 0 && 2 * rem < zc && bnz > zc) {
             bnz -= rem;
             ibox[5] -= rem;
             t.e[2] = ibox[5];
