@@ -296,12 +296,15 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         }
         // z faces: on 16-cell boundaries where a staged interior reads a
         // one-byte material index map (its tensor-map x coordinate is in
-        // bytes), else on vector-width boundaries (the field maps' x
-        // coordinate, 3 k esize / 8, is then even); the staged interior is
-        // the automatic one for float32 with compact materials
+        // bytes), and for float fields (a row start on a 32-byte sector
+        // boundary: config 5 float32c 0.804 vs 0.832 ms per step with the
+        // interior from z = 20); float64 on 4-cell boundaries (96 bytes; the
+        // field maps' x coordinate, 3 k esize / 8, is then even; config 5
+        // float64 2.42 vs 2.47 ms with 12 fewer shell cells per z face)
         const bool stg = d->variant == 2 || (d->variant == 0 && d->precision == FDTD_FLOAT32 &&
                                               mat_want[0] != MAT_FULL && mat_want[1] != MAT_FULL);
-        const int za = stg && (mat_want[0] == MAT_IDS || mat_want[1] == MAT_IDS) ? 16 : vmax;
+        const bool idx = stg && (mat_want[0] == MAT_IDS || mat_want[1] == MAT_IDS);
+        const int za = idx || d->precision != FDTD_FLOAT64 ? 16 : 4;
         lo[2] = (lo[2] + za - 1) / za * za;
         hi[2] = hi[2] / vmax * vmax;
         const bool inner = lo[0] < hi[0] && lo[1] < hi[1] && lo[2] < hi[2];
