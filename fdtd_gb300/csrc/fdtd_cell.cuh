@@ -20,35 +20,7 @@ struct PsiSrc {
     int row;                     // this thread's row in the tile
     int k0c;                     // first cell of the tile along z
     const T *ctab;               // b/c tables at g.coef_off[s] (null: global)
-    const T *pre;                // the pairs of slab pre_slab, already loaded (null: none)
-    int pre_slab;
 };
-
-// The auxiliary pairs of a thread's V cells in slab s, loaded from global
-// memory into pre[2V] (pairs of cells outside the slab read as zero), so
-// that a kernel can issue these loads together with its field loads.
-template <class T, int V, bool IS_E>
-__device__ __forceinline__ void load_pml_pairs(const GridK &g, int s, int i, int j, int k0, T (&pre)[2 * V]) {
-    const SlabK &S = g.slab[s];
-    const T *psi = (const T *)(IS_E ? S.psiE : S.psiH);
-    const int a = S.axis;
-    const int l0 = (a == 0 ? i : (a == 1 ? j : k0)) - S.start;
-#pragma unroll
-    for (int q = 0; q < 2 * V; ++q) pre[q] = T(0);
-    if (a != 2) {
-        const long gofs = a == 0 ? ((long)l0 * g.ny + j) * g.nz + k0 : ((long)i * S.th + l0) * g.nz + k0;
-#pragma unroll
-        for (int q = 0; q < 2 * V; ++q) pre[q] = psi[2 * gofs + q];
-    } else {
-        const long gofs = ((long)i * g.ny + j) * S.thp + l0;
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            if ((unsigned)(l0 + v) >= (unsigned)S.th) continue;
-            pre[2 * v] = psi[2 * (gofs + v)];
-            pre[2 * v + 1] = psi[2 * (gofs + v) + 1];
-        }
-    }
-}
 
 // Bit s set: PML slab s can contain cells of this thread.  The y and z parts
 // do not change along x (computed once per thread), the x part per plane.
@@ -280,16 +252,9 @@ __device__ __forceinline__ void apply_pml_slab(const GridK &g, int s, int i, int
     // all loads first (a store to the auxiliaries would otherwise order every
     // later load behind it), then the updates, then the stores
     T p0[V], p1[V];
-    const T *pre = src.pre && s == src.pre_slab ? src.pre : nullptr;
     if constexpr (A != 2) {
         // x/y slab: the V cells share one slab-local index
-        if (pre) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                p0[v] = pre[2 * v];
-                p1[v] = pre[2 * v + 1];
-            }
-        } else if constexpr (V > 1) {
+        if constexpr (V > 1) {
             // one contiguous, 16-byte aligned run of pairs
             alignas(16) T pr[2 * V];
             if (sp) ld_vec(pr, sp);
@@ -346,10 +311,7 @@ __device__ __forceinline__ void apply_pml_slab(const GridK &g, int s, int i, int
             p0[v] = T(0);
             p1[v] = T(0);
             if ((unsigned)l >= (unsigned)th) continue;
-            if (pre) {
-                p0[v] = pre[2 * v];
-                p1[v] = pre[2 * v + 1];
-            } else if (sp) {
+            if (sp) {
                 p0[v] = sp[2 * v];
                 p1[v] = sp[2 * v + 1];
             } else {

@@ -276,12 +276,6 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
     const T *__restrict__ H = (const T *)g.H;
     T *E = (T *)g.E;
     T *Elo = (T *)g.Elo;
-    // the first slab's auxiliary pairs, loaded with the fields (one memory
-    // round trip instead of two)
-    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
-    const int s0 = slabs ? __ffs(slabs) - 1 : -1;
-    alignas(16) T pre[2 * V];
-    if (s0 >= 0) load_pml_pairs<T, V, true>(g, s0, i, j, k0, pre);
     alignas(16) T hc[N], hp[N], hj[N], e[N], el[N], m[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
@@ -303,8 +297,9 @@ __global__ void __launch_bounds__(kThreads) k_shell_E(const GridK g, const Shell
         sb0 = g.srcE_off[cta];
         sb1 = g.srcE_off[cta + 1];
     }
-    const PsiSrc<T> src{nullptr, 0, 0, nullptr, s0 >= 0 ? pre : nullptr, s0};
-    thread_E<P, V>(g, wave, i, j, k0, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, src,
+    const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
+    thread_E<P, V>(g, wave, i, j, k0, courant_of<T>(g), hc, hp, hj, kx, ky, m, e, el, ob0, ob1, sb0, sb1, nostage,
                    slabs);
     shell_st(E + 3 * cell0, e);
     if constexpr (P::COMP) shell_st(Elo + 3 * cell0, el);
@@ -322,10 +317,6 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
     const T *__restrict__ E = (const T *)g.E;
     T *H = (T *)g.H;
     T *Hlo = (T *)g.Hlo;
-    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
-    const int s0 = slabs ? __ffs(slabs) - 1 : -1;
-    alignas(16) T pre[2 * V];
-    if (s0 >= 0) load_pml_pairs<T, V, false>(g, s0, i, j, k0, pre);
     alignas(16) T ec[N], en[N], ej[N], h[N], hl[N], m[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
@@ -347,8 +338,9 @@ __global__ void __launch_bounds__(kThreads) k_shell_H(const GridK g, const Shell
         sb0 = g.srcH_off[cta];
         sb1 = g.srcH_off[cta + 1];
     }
-    const PsiSrc<T> src{nullptr, 0, 0, nullptr, s0 >= 0 ? pre : nullptr, s0};
-    thread_H<P, V>(g, wave, i, j, k0, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, src, slabs);
+    const PsiSrc<T> nostage{nullptr, 0, 0, nullptr};
+    const unsigned slabs = shell_mask<V>(g, cand, i, j, k0);
+    thread_H<P, V>(g, wave, i, j, k0, courant_of<T>(g), ec, en, ej, kx, ky, m, h, hl, sb0, sb1, nostage, slabs);
     shell_st(H + 3 * cell0, h);
     if constexpr (P::COMP) shell_st(Hlo + 3 * cell0, hl);
 }
