@@ -278,7 +278,7 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
     // cell the bulk pass has just written), and each cell still gets bulk,
     // objects, slabs in registration order and sources in that order, as in
     // every mode.  Automatic on grids of 8M cells or more whose shell holds
-    // at least a fifth of the cells (float32 ms per step, split slabs vs
+    // at least a fifth of the cells, a tenth in float64 (float32 ms per step, split slabs vs
     // partition: config 2 0.443 vs 0.375, config 5 0.618 vs 0.608; float64
     // config 2 1.74 vs 1.49; float32c config 5 1.10 vs 0.85; config 3, 12 %
     // of its cells in the shell, stays faster with its slabs split: 5.47 vs
@@ -312,8 +312,12 @@ static int create(const fdtd_grid_desc *d, Plan &p) {
         if (pml_base == 4 && !ok) return FDTD_ERR_UNSUPPORTED;
         bool want = ok && pml_base == 4;
         if (ok && pml_base == 0 && ncell >= (8L << 20)) {
+            // a fifth of the cells in the shell; float64 (arithmetic bound,
+            // register-streaming interior) from a tenth (config 3: 29.1 vs
+            // 30.4 ms per step)
             const long inside = (long)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
-            want = 5 * (ncell - inside) >= ncell;
+            const long frac = d->precision == FDTD_FLOAT64 ? 10 : 5;
+            want = frac * (ncell - inside) >= ncell;
         }
         if (want) {
             for (int a = 0; a < 3; ++a) {

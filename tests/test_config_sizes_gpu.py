@@ -103,13 +103,14 @@ def test_config1_full_size_float32(fd, c1_oracle, c1_fixture, prec, plan):
 # crops: builder, steps, full-size plan per precision, anisotropic (no bit identity)
 # the plans the full-size grids get: configs 2 and 5 the interior/shell
 # partition (register-streaming interior, or the staged one for float32 with
-# compact materials), config 3 its slabs in kernels of their own
+# compact materials), config 3 its slabs in kernels of their own (float64:
+# the partition)
 CROPS = {
     "c2_128": (lambda m: scenes.c2(m, n=128, pml=8), 8,
                {"float64": dict(variant=1, pml_mode=4), "float32": dict(variant=1, pml_mode=4),
                 "float32c": dict(variant=1, pml_mode=4)}, False),
     "c3_192": (lambda m: scenes.c3(m, n=192, pml=5, detector=True), 8,
-               {"float64": dict(variant=2, pml_mode=2, tile_rows=8),
+               {"float64": dict(variant=1, pml_mode=4),
                 "float32": dict(variant=2, pml_mode=3, tile_rows=8),
                 "float32c": dict(variant=2, pml_mode=2, tile_rows=8)}, False),
     "c5_192x192x96": (lambda m: scenes.c5(m, nx=192, ny=192, nz=96, pml=10), 8,
