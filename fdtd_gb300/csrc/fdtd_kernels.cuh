@@ -635,29 +635,11 @@ __global__ void k_dft(const T *__restrict__ E, const T *__restrict__ Elo, int ny
         const size_t at = 3 * (((size_t)i * ny + j) * nz + k) + comp;
         double e = (double)E[at];
         if constexpr (COMP) e = e + (double)Elo[at];
-        // up to four frequencies at a time: every accumulator load first (the
-        // stores could alias later loads, so the compiler would otherwise
-        // wait for each read-modify-write in turn)
-        constexpr int FB = 4;
-        for (int f0 = 0; f0 < d.n_freq; f0 += FB) {
-            const int nf = min(FB, d.n_freq - f0);
-            double re[FB], im[FB];
-#pragma unroll
-            for (int q = 0; q < FB; ++q) {
-                if (q >= nf) continue;
-                const double *acc = d.acc + 2 * ((size_t)(f0 + q) * ncell * 3 + t);
-                re[q] = acc[0];
-                im[q] = acc[1];
-            }
-#pragma unroll
-            for (int q = 0; q < FB; ++q) {
-                if (q >= nf) continue;
-                const int f = f0 + q;
-                const double cs = phase[2 * (d.phase_offset + f)], sn = phase[2 * (d.phase_offset + f) + 1];
-                double *acc = d.acc + 2 * ((size_t)f * ncell * 3 + t);
-                acc[0] = __dadd_rn(re[q], __dmul_rn(e, cs));
-                acc[1] = __dadd_rn(im[q], __dmul_rn(e, sn));
-            }
+        for (int f = 0; f < d.n_freq; ++f) {
+            const double cs = phase[2 * (d.phase_offset + f)], sn = phase[2 * (d.phase_offset + f) + 1];
+            double *acc = d.acc + 2 * ((size_t)f * ncell * 3 + t);
+            acc[0] = __dadd_rn(acc[0], __dmul_rn(e, cs));
+            acc[1] = __dadd_rn(acc[1], __dmul_rn(e, sn));
         }
     }
 }
