@@ -96,7 +96,7 @@ def parse():
                    help="skip configs 2 and 5 (forward throughput, roofline and long-run errors)")
     p.add_argument("--step-fusion", type=int, default=0,
                    help="0 auto, 1 two passes per step, 2 one pass per step (float32 grids that allow it)")
-    p.add_argument("--forward-only", choices=["c2", "c5"], default=None,
+    p.add_argument("--forward-only", choices=["c1", "c2", "c4", "c5"], default=None,
                    help="only --warmup + --steps float32 forward steps of the named config (a profiling target; "
                         "prints its own JSON line)")
     p.add_argument("--configs-only", action="store_true",
@@ -804,7 +804,11 @@ def main():
         from fdtd_gb300 import scenes
 
         fd.set_backend("gb300.float32")
-        if args.forward_only == "c2":
+        if args.forward_only == "c1":
+            g = scenes.c1(fd)
+        elif args.forward_only == "c4":
+            g = scenes.c4(fd)
+        elif args.forward_only == "c2":
             g = scenes.c2(fd, n=208, pml=13) if args.small else scenes.c2(fd)
         else:
             g = scenes.c5(fd, nx=256, ny=256) if args.small else scenes.c5(fd)
